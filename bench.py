@@ -1,0 +1,504 @@
+#!/usr/bin/env python3
+"""Gate-throughput benchmark of the GB300 state-vector core.
+
+Workload (one GPU): the gate-throughput sweep on a 30-qubit complex128 state
+(16 GiB, wire 0 = most significant bit) prepared by a Hadamard layer.  One
+step applies, for each of PauliX, Hadamard, RX, CNOT, CRY, IsingXX,
+SingleExcitation, DoubleExcitation and a Haar-random two-qubit matrix, `reps`
+applications on distinct wires drawn from each of the low (0-4), mid (12-17)
+and high (25-29) wire ranges, angles uniform in [0, 2*pi) (seed 2).
+
+Metric: algorithmic HBM GB/s = sum over applications of touched_fraction x
+2 x 2^30 x 16 B (read + write) / device time.  The state (16 GiB) is far
+larger than L2 (129 MB), so no L2 flush is needed between applications.
+
+Printed JSON line:
+  value      - device-resident throughput (CUDA events on the state's stream)
+  e2e        - the same metric through the reference-facing pybind API
+               (LightningKokkos_C128) with the state copied from pinned host
+               memory before and back after every step
+  roofline   - the gate kernel with the largest time share, against the
+               measured HBM copy bandwidth
+  per_gate   - GB/s and time share of every gate type (and wire range)
+  cpu_baseline - the oracle (CPU restatement of the reference functors) on
+               the host cores, a bounded sample of the same sweep
+  adjoint_26q - adjoint Jacobian of the 26-qubit ansatz (40 layers of RY, RZ
+               + CNOT ladder, 100-term Pauli Hamiltonian) in complex64 with
+               FP64 accumulation vs complex128, seconds per gradient and the
+               largest gradient difference
+`--impl reference` times the oracle instead.  For --gpus N
+under torchrun every rank runs an independent replica (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "pennylane-lightning-kokkos_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "gate HBM GB/s vs peak; adjoint grad s/circuit c64+FP64-acc vs c128 at stated err"
+GIB = 1 << 30
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--nq", type=int, default=30)
+    ap.add_argument("--reps", type=int, default=4, help="applications per gate and wire range per step")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-nq", type=int, default=26)
+    ap.add_argument("--adjoint-layers", type=int, default=40)
+    return ap.parse_args(argv)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- clocks --
+class ClockSampler:
+    FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device):
+        self.device, self.lines, self.proc, self.err = device, [], None, None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + ",".join(self.FIELDS), "--format=csv,noheader,nounits", "-lms",
+                 "200", "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception as e:  # nvidia-smi missing
+            self.err = str(e)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"unavailable": self.err or "nvidia-smi not started"}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"unavailable": "no samples"}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ device sweep --
+class SweepRunner:
+    """Applies a gate-sweep plan to a device-resident state through the C ABI."""
+
+    def __init__(self, nq, plan, device, stream):
+        from pennylane_lightning_kokkos import _native as N
+
+        self.N, self.nq, self.plan = N, nq, plan
+        h = C.c_void_p()
+        N.check(N.lib.plk_state_create(nq, N.PLK_C128, device, C.byref(h)))
+        self.h = h
+        N.check(N.lib.plk_state_set_stream(h, C.c_void_p(stream.cuda_stream)))
+        self.keep, self.calls = [], []
+        for app in plan:
+            w = np.array(app["wires"], dtype=np.int64)
+            self.keep.append(w)
+            wp = w.ctypes.data_as(C.POINTER(C.c_int64))
+            if app["matrix"] is not None:
+                m = np.ascontiguousarray(app["matrix"], dtype=np.complex128)
+                self.keep.append(m)
+                self.calls.append(("m", m.ctypes.data_as(C.POINTER(C.c_double)), wp, len(w)))
+            else:
+                p = np.array(app["params"] or [0.0], dtype=np.float64)
+                self.keep.append(p)
+                self.calls.append(("g", N.GATE_ID[app["name"]], wp, len(w), p.ctypes.data_as(C.POINTER(C.c_double)),
+                                   len(app["params"])))
+        # |+>^n: Hadamard on every wire
+        for wire in range(nq):
+            w = np.array([wire], dtype=np.int64)
+            N.check(N.lib.plk_apply_gate(h, N.GATE_ID["Hadamard"], w.ctypes.data_as(C.POINTER(C.c_int64)), 1, 0,
+                                         None, 0))
+
+    def apply(self, i):
+        c = self.calls[i]
+        if c[0] == "m":
+            st = self.N.lib.plk_apply_matrix(self.h, c[1], c[2], c[3], 0)
+        else:
+            st = self.N.lib.plk_apply_gate(self.h, c[1], c[2], c[3], 0, c[4], c[5])
+        if st:
+            self.N.check(st)
+
+    def close(self):
+        self.N.lib.plk_state_destroy(self.h)
+
+
+def run_device_sweep(args, device, torch, dist_barrier):
+    from pennylane_lightning_kokkos.circuits import gate_sweep_plan
+
+    plan = gate_sweep_plan(args.nq, args.reps, seed=2)
+    stream = torch.cuda.Stream(device=device)
+    runner = SweepRunner(args.nq, plan, device, stream)
+    amp = 2 * (1 << args.nq) * 16  # bytes read + written for the full state
+    groups = []  # (gate name, [plan indices])
+    for i, app in enumerate(plan):
+        if not groups or groups[-1][0] != app["name"]:
+            groups.append((app["name"], []))
+        groups[-1][1].append(i)
+    range_groups = {}
+    for i, app in enumerate(plan):
+        range_groups.setdefault((app["name"], app["range"]), []).append(i)
+
+    def step(events=None):
+        for gi, (_, idx) in enumerate(groups):
+            if events is not None:
+                events[gi].record(stream)
+            for i in idx:
+                runner.apply(i)
+        if events is not None:
+            events[-1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(device)
+    clocks = ClockSampler(device)
+    clocks.start()
+    time.sleep(0.3)
+    dist_barrier()
+    torch.cuda.synchronize(device)
+    mk = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    t0, t1 = mk(), mk()
+    step_events = [[mk() for _ in range(len(groups) + 1)] for _ in range(args.steps)]
+    t0.record(stream)
+    for k in range(args.steps):
+        step(step_events[k])
+    t1.record(stream)
+    torch.cuda.synchronize(device)
+    dist_barrier()
+    clk = clocks.stop()
+    total_ms = t0.elapsed_time(t1)
+    per_gate_ms = {g: 0.0 for g, _ in groups}
+    for k in range(args.steps):
+        ev = step_events[k]
+        for gi, (g, _) in enumerate(groups):
+            per_gate_ms[g] += ev[gi].elapsed_time(ev[gi + 1])
+    bytes_per_gate = {g: sum(plan[i]["touched"] * amp for i in idx) * args.steps for g, idx in groups}
+    total_bytes = sum(bytes_per_gate.values())
+    # per (gate, range) timing: one extra untimed-for-value pass with events per range
+    rng_ms = {}
+    ev = {key: (mk(), mk()) for key in range_groups}
+    for key, idx in range_groups.items():
+        ev[key][0].record(stream)
+        for i in idx:
+            runner.apply(i)
+        ev[key][1].record(stream)
+    torch.cuda.synchronize(device)
+    for key, (a, b) in ev.items():
+        ms = a.elapsed_time(b)
+        nbytes = sum(plan[i]["touched"] * amp for i in range_groups[key])
+        rng_ms[f"{key[0]}/{key[1]}"] = {"ms_per_app": ms / len(range_groups[key]),
+                                       "GBps": nbytes / (ms * 1e6)}
+    runner.close()
+    return {
+        "plan": plan, "groups": groups, "total_ms": total_ms, "per_gate_ms": per_gate_ms,
+        "bytes_per_gate": bytes_per_gate, "total_bytes": total_bytes, "clocks": clk, "per_range": rng_ms,
+        "launches": len(plan) * args.steps,
+    }
+
+
+# -------------------------------------------------------------------- e2e --
+def run_e2e(args, device, torch, plan, steps):
+    import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
+
+    n = 1 << args.nq
+    host_t = torch.empty(n, dtype=torch.complex128, pin_memory=True)
+    host = host_t.numpy()
+    host[:] = 1.0 / np.sqrt(n)
+    sv = m.LightningKokkos_C128(args.nq, m.InitializationSettings().set_device_id(device))
+    names = [a["name"] for a in plan]
+    amp = 2 * n * 16
+
+    def one_step():
+        sv.HostToDevice(host)
+        for a in plan:
+            if a["matrix"] is not None:
+                sv.apply("QubitUnitary", a["wires"], False, [[]], a["matrix"])
+            else:
+                getattr(sv, a["name"])(a["wires"], False, a["params"])
+        sv.DeviceToHost(host)
+
+    one_step()  # warm-up
+    t = time.perf_counter()
+    for _ in range(steps):
+        one_step()
+    dt = time.perf_counter() - t
+    nbytes = sum(a["touched"] * amp for a in plan) * steps
+    del sv
+    return {"value": nbytes / dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 16,
+            "steps": steps, "api": "lightning_kokkos_qubit_ops.LightningKokkos_C128 (pinned host buffer)",
+            "gates_per_step": len(names)}
+
+
+# ------------------------------------------------------------- CPU legs --
+def oracle_sweep(nq, plan, threads):
+    import oracle as O
+
+    O.set_num_threads(threads)
+    n = 1 << nq
+    sv = np.full(n, 1.0 / np.sqrt(n), dtype=np.complex128)
+    amp = 2 * n * 16
+    t = time.perf_counter()
+    nbytes = 0.0
+    for a in plan:
+        if a["matrix"] is not None:
+            O.apply_matrix(sv, a["matrix"], a["wires"])
+        else:
+            O.apply(sv, a["name"], a["wires"], False, a["params"])
+        nbytes += a["touched"] * amp
+    dt = time.perf_counter() - t
+    return nbytes / dt / 1e9, dt
+
+
+def run_cpu_baseline(args):
+    from pennylane_lightning_kokkos.circuits import gate_sweep_plan
+
+    threads = os.cpu_count() or 1
+    plan = gate_sweep_plan(args.nq, 1, seed=2)
+    gbs, dt = oracle_sweep(args.nq, plan, threads)
+    return {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"{len(plan)} applications (1 per gate x wire range) on the {args.nq}-qubit complex128 "
+                      f"state, OpenMP oracle, {dt:.1f} s"}
+
+
+def run_reference_arm(args, rank):
+    """--impl reference: the oracle (plain-C restatement of the reference's
+    Kokkos functors, OpenMP on every host core) on the same sweep; each step
+    is one application per gate type, cycling through the wire ranges."""
+    from pennylane_lightning_kokkos.circuits import gate_sweep_plan, wire_ranges
+
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    ranges = list(wire_ranges(args.nq))
+    full = gate_sweep_plan(args.nq, max(1, args.steps + args.warmup), seed=2)
+    by_key = {}
+    for a in full:
+        by_key.setdefault((a["name"], a["range"]), []).append(a)
+    steps = []
+    for k in range(args.warmup + args.steps):
+        r = ranges[k % len(ranges)]
+        steps.append([by_key[(g, r)][k // len(ranges)] for g in dict.fromkeys(a["name"] for a in full)])
+    import oracle as O
+
+    O.set_num_threads(threads)
+    n = 1 << args.nq
+    sv = np.full(n, 1.0 / np.sqrt(n), dtype=np.complex128)
+    amp = 2 * n * 16
+    for s in steps[:args.warmup]:
+        for a in s:
+            if a["matrix"] is not None:
+                O.apply_matrix(sv, a["matrix"], a["wires"])
+            else:
+                O.apply(sv, a["name"], a["wires"], False, a["params"])
+    t = time.perf_counter()
+    nbytes = 0.0
+    for s in steps[args.warmup:]:
+        for a in s:
+            if a["matrix"] is not None:
+                O.apply_matrix(sv, a["matrix"], a["wires"])
+            else:
+                O.apply(sv, a["name"], a["wires"], False, a["params"])
+            nbytes += a["touched"] * amp
+    dt = time.perf_counter() - t
+    value = nbytes / dt / 1e9
+    return {
+        "metric": METRIC, "value": value, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / max(1, args.steps),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)",
+        "data": "synthetic (seeded gate sweep, seed 2)",
+        "config": {"workload": f"gate sweep, {args.nq} qubits complex128, 9 gate types x low/mid/high wires",
+                   "step": "one application per gate type, wire range cycling low/mid/high"},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} steps x 9 applications, OpenMP oracle"},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+# ------------------------------------------------------------ adjoint 26q --
+def run_adjoint(args, device, torch):
+    import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
+    from pennylane_lightning_kokkos.circuits import hardware_efficient_ansatz, random_pauli_words
+
+    nq, layers = args.adjoint_nq, args.adjoint_layers
+    ops = hardware_efficient_ansatz(nq, layers, seed=4, rotations=("RY", "RZ"), entangler="ladder")
+    words = random_pauli_words(nq, 100, seed=4)
+    npar = sum(1 for o in ops if o[3])
+    out = {"qubits": nq, "layers": layers, "params": npar, "ops": len(ops), "hamiltonian_terms": len(words)}
+    grads = {}
+    for bits in ("128", "64"):
+        dt = np.float64 if bits == "128" else np.float32
+        cdt = np.complex128 if bits == "128" else np.complex64
+        L = lambda name: getattr(m, name + "_C" + bits)  # noqa: E731
+        letters = {"X": "PauliX", "Y": "PauliY", "Z": "PauliZ"}
+        terms = []
+        for c, w, l in words:
+            fac = [L("NamedObsKokkos")(letters[x], [wi]) for wi, x in zip(w, l)]
+            terms.append(fac[0] if len(fac) == 1 else L("TensorProdObsKokkos")(fac))
+        ham = L("HamiltonianKokkos")(np.array([c for c, _, _ in words], dtype=dt), terms)
+        adj = L("AdjointJacobianKokkos")()
+        tape = adj.create_ops_list([o[0] for o in ops], [np.array(o[3], dtype=dt) for o in ops], [o[1] for o in ops],
+                                   [o[2] for o in ops], [np.array([], dtype=cdt)] * len(ops))
+        names, wires, invs, prms = [o[0] for o in ops], [o[1] for o in ops], [o[2] for o in ops], [o[3] for o in ops]
+
+        def gradient():
+            sv = L("LightningKokkos")(nq, m.InitializationSettings().set_device_id(device))
+            sv.apply(names, wires, invs, prms)
+            return np.asarray(adj.adjoint_jacobian(sv, [ham], tape, list(range(npar))), dtype=np.float64)[0]
+
+        gradient()  # warm-up (allocator pools, module load)
+        torch.cuda.synchronize(device)
+        reps = 2
+        t = time.perf_counter()
+        for _ in range(reps):
+            g = gradient()
+        torch.cuda.synchronize(device)
+        out[f"c{bits}_s_per_gradient"] = (time.perf_counter() - t) / reps
+        grads[bits] = g
+    out["c64_speedup_vs_c128"] = out["c128_s_per_gradient"] / out["c64_s_per_gradient"]
+    out["max_abs_grad_diff_c64_vs_c128"] = float(np.max(np.abs(grads["64"] - grads["128"])))
+    out["error_reference"] = "complex128 GPU path (parity-checked against the FP64 oracle at <= 20 qubits)"
+    return out
+
+
+# ------------------------------------------------------------------ main --
+def main(argv=None):
+    args = parse_args(argv)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        res = run_reference_arm(args, rank)
+        if res is not None:
+            print(json.dumps(res), flush=True)
+        return 0
+
+    import torch
+
+    device = local_rank
+    torch.cuda.set_device(device)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", device))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    sweep = run_device_sweep(args, device, torch, barrier)
+    total_ms = sweep["total_ms"]
+    total_bytes = sweep["total_bytes"]
+    if dist is not None:
+        t = torch.tensor([total_ms, total_bytes], dtype=torch.float64, device=f"cuda:{device}")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        sm = t.clone()
+        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+        total_ms, total_bytes = float(mx[0]), float(sm[1])
+    value = total_bytes / (total_ms * 1e6)
+
+    peak, peak_kind = peaks()
+    shares = {g: ms / sweep["total_ms"] for g, ms in sweep["per_gate_ms"].items()}
+    per_gate = {g: {"GBps": sweep["bytes_per_gate"][g] / (ms * 1e6), "share": shares[g],
+                    "ms_per_app": ms / (args.steps * sum(1 for a in sweep["plan"] if a["name"] == g))}
+                for g, ms in sweep["per_gate_ms"].items()}
+    dom = max(shares, key=shares.get)
+    n_apps_dom = sum(1 for a in sweep["plan"] if a["name"] == dom) * args.steps
+    roof = {"bound": "hbm", "kernel": f"{dom} gate kernel",
+            "achieved": per_gate[dom]["GBps"], "peak": peak, "unit": "GB/s",
+            "frac": per_gate[dom]["GBps"] / peak, "peak_kind": peak_kind,
+            "traffic": None, "launches": n_apps_dom,
+            "overall_frac": value / (peak * world)}
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            tr = json.load(open(prof)).get(dom)
+            if tr:
+                roof["traffic"] = tr
+        except Exception:
+            pass
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic (seeded gate sweep, seed 2)",
+        "config": {"workload": f"gate sweep, {args.nq} qubits complex128 ({(1 << args.nq) * 16 / GIB:.0f} GiB state), "
+                               "9 gate types x low/mid/high wire ranges",
+                   "applications_per_step": len(sweep["plan"]), "reps_per_gate_and_range": args.reps,
+                   "l2": "state larger than L2 (129 MB): no flush needed",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roof, "per_gate": per_gate, "per_range": sweep["per_range"], "clocks": sweep["clocks"],
+        "gpu_launches": sweep["launches"],
+    }
+    if rank == 0 and not args.no_e2e:
+        result["e2e"] = run_e2e(args, device, torch, sweep["plan"], steps=max(1, min(args.steps, 3)))
+    if rank == 0 and not args.no_adjoint:
+        try:
+            result["adjoint_26q"] = run_adjoint(args, device, torch)
+        except Exception as e:  # report, do not hide the main number
+            result["adjoint_26q"] = {"error": repr(e)}
+    if rank == 0 and not args.no_cpu:
+        result["cpu_baseline"] = run_cpu_baseline(args)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,228 @@
+/*
+ * plk_gb300.h — C ABI of the GB300 state-vector core.
+ *
+ * A drop-in replacement for the device path under the LightningKokkos
+ * plugin: the C++ host layer (state, measures, observables, adjoint
+ * Jacobian) and the pybind11 module `lightning_kokkos_qubit_ops` call these
+ * functions, which run hand-written sm_103a CUDA kernels.  Each declaration
+ * names the reference entry point it replaces (paths relative to
+ * pennylane_lightning_kokkos/src/).
+ *
+ * Conventions
+ *   - A state holds 2^num_qubits amplitudes, complex64 (PLK_C64) or
+ *     complex128 (PLK_C128), contiguous, wire 0 = most significant bit of the
+ *     amplitude index (the reference's rev_wire = n - wire - 1).
+ *   - Every function returns a plk_status; on failure plk_last_error()
+ *     returns a message (thread-local) and the state is left unchanged
+ *     unless stated otherwise.
+ *   - Matrices are complex128, row-major, interleaved (re, im), whatever the
+ *     state precision; a k-wire matrix has 4^k entries and wires[0] is the
+ *     most significant bit of its row/column index.
+ *   - Reductions (expectation values, inner products, Jacobian entries)
+ *     accumulate in FP64 for both precisions and are deterministic: the same
+ *     inputs on the same GPU give the same bits.
+ *   - Host pointers may be pageable or pinned; device work for a state is
+ *     issued on the state's stream (plk_state_set_stream).  Functions that
+ *     return host values synchronize that stream.
+ */
+#ifndef PLK_GB300_H
+#define PLK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PLK_API __attribute__((visibility("default")))
+
+typedef enum {
+    PLK_OK = 0,
+    PLK_ERR_INVALID_ARG = 1,  /* bad wires, sizes, names, parameters        */
+    PLK_ERR_UNKNOWN_GATE = 2, /* name/id without a kernel (or generator)     */
+    PLK_ERR_CUDA = 3,         /* a CUDA runtime call failed                 */
+    PLK_ERR_OUT_OF_MEMORY = 4,
+    PLK_ERR_UNSUPPORTED = 5,  /* valid request outside this build's limits  */
+    PLK_ERR_NO_DEVICE = 6
+} plk_status;
+
+typedef enum { PLK_C64 = 0, PLK_C128 = 1 } plk_dtype;
+
+/* Gate identifiers: the gate map of StateVectorKokkos.hpp:141-344 plus
+ * Identity (a no-op, :589-590) and PLK_GATE_MATRIX (applyMultiQubitOp). */
+typedef enum {
+    PLK_GATE_IDENTITY = 0,
+    PLK_GATE_PAULIX, PLK_GATE_PAULIY, PLK_GATE_PAULIZ, PLK_GATE_HADAMARD,
+    PLK_GATE_S, PLK_GATE_T, PLK_GATE_PHASESHIFT, PLK_GATE_RX, PLK_GATE_RY,
+    PLK_GATE_RZ, PLK_GATE_ROT,
+    PLK_GATE_CNOT, PLK_GATE_CY, PLK_GATE_CZ, PLK_GATE_SWAP,
+    PLK_GATE_CONTROLLEDPHASESHIFT, PLK_GATE_CRX, PLK_GATE_CRY, PLK_GATE_CRZ,
+    PLK_GATE_CROT, PLK_GATE_ISINGXX, PLK_GATE_ISINGXY, PLK_GATE_ISINGYY,
+    PLK_GATE_ISINGZZ, PLK_GATE_SINGLEEXCITATION,
+    PLK_GATE_SINGLEEXCITATIONMINUS, PLK_GATE_SINGLEEXCITATIONPLUS,
+    PLK_GATE_DOUBLEEXCITATION, PLK_GATE_DOUBLEEXCITATIONMINUS,
+    PLK_GATE_DOUBLEEXCITATIONPLUS, PLK_GATE_CSWAP, PLK_GATE_TOFFOLI,
+    PLK_GATE_MULTIRZ,
+    PLK_GATE_MATRIX, /* dense 2^k x 2^k matrix in plk_op.matrix */
+    PLK_GATE_COUNT
+} plk_gate;
+
+typedef struct plk_state_s *plk_state;
+
+/* One operation of a circuit (the serialised tape of OpsData,
+ * algorithms/AdjointDiffKokkos.hpp:17-173). */
+typedef struct {
+    int32_t gate;        /* plk_gate                                        */
+    int32_t num_wires;
+    int32_t adjoint;     /* apply the inverse gate                          */
+    int32_t num_params;
+    const int64_t *wires;
+    const double *params;
+    const double *matrix; /* PLK_GATE_MATRIX only: 4^num_wires complex128   */
+} plk_op;
+
+typedef struct {
+    int device;
+    int sm_count;
+    int cc_major;
+    int cc_minor;
+    uint64_t total_mem;
+    uint64_t free_mem;
+    int clock_khz;
+    int mem_clock_khz;
+    int mem_bus_width;
+    char name[128];
+} plk_device_info;
+
+/* ---- library ---------------------------------------------------------- */
+/* Thread-local message of the last failure (never NULL). */
+PLK_API const char *plk_last_error(void);
+PLK_API int plk_version(void);
+/* Replaces GetConfigInfo.hpp:64 getConfig / Kokkos::print_configuration
+ * (bindings/Bindings.cpp:842-852) with a CUDA device description. */
+PLK_API int plk_device_count(int *count);
+PLK_API int plk_get_device_info(int device, plk_device_info *out);
+/* Name -> plk_gate (the string keys of StateVectorKokkos.hpp:141-344). */
+PLK_API int plk_gate_from_name(const char *name, int32_t *gate);
+PLK_API int plk_gate_num_wires(int32_t gate);   /* -1: any number */
+PLK_API int plk_gate_num_params(int32_t gate);
+
+/* ---- state lifecycle (StateVectorKokkos.hpp:140-574, 1596-1636) ------- */
+/* StateVectorKokkos(num_qubits): allocate and set |0...0> (InitView :46). */
+PLK_API int plk_state_create(int num_qubits, int dtype, int device, plk_state *out);
+/* Wrap caller-owned device memory (2^num_qubits amplitudes); the state does
+ * not free it.  stream may be NULL (library stream of the device). */
+PLK_API int plk_state_wrap(void *device_ptr, int num_qubits, int dtype, int device,
+                           void *cuda_stream, plk_state *out);
+PLK_API int plk_state_destroy(plk_state s);
+PLK_API int plk_state_get(plk_state s, int *num_qubits, int *dtype, void **device_ptr);
+PLK_API int plk_state_set_stream(plk_state s, void *cuda_stream);
+PLK_API int plk_state_get_stream(plk_state s, void **cuda_stream);
+PLK_API int plk_state_synchronize(plk_state s);
+/* resetStateVector :508-512 */
+PLK_API int plk_state_reset(plk_state s);
+/* initZeros :483-485 */
+PLK_API int plk_state_zero(plk_state s);
+/* setBasisState :492-495 */
+PLK_API int plk_state_set_basis(plk_state s, uint64_t index);
+/* setStateVector :503-521: zero, then scatter values (host arrays, values in
+ * the state precision, interleaved re/im). */
+PLK_API int plk_state_set_values(plk_state s, const uint64_t *indices, const void *values,
+                                 uint64_t count);
+/* HostToDevice / DeviceToHost :1618-1628 (length in amplitudes, state
+ * precision). */
+PLK_API int plk_state_h2d(plk_state s, const void *host, uint64_t length);
+PLK_API int plk_state_d2h(plk_state s, void *host, uint64_t length);
+/* DeviceToDevice / updateData :1596-1598, :1631-1633 */
+PLK_API int plk_state_copy(plk_state dst, plk_state src);
+/* axpy_Kokkos (util/LinearAlgebraKokkos.hpp:30-61): y += alpha * x */
+PLK_API int plk_state_axpy(plk_state y, double alpha_re, double alpha_im, plk_state x);
+
+/* ---- gates ------------------------------------------------------------ */
+/* applyOperation :585-600 (named gate, adjoint flag, parameters). */
+PLK_API int plk_apply_gate(plk_state s, int32_t gate, const int64_t *wires, int32_t num_wires,
+                           int32_t adjoint, const double *params, int32_t num_params);
+/* applyMultiQubitOp :757-796 (and single/two-qubit op :704-748). */
+PLK_API int plk_apply_matrix(plk_state s, const double *matrix, const int64_t *wires,
+                             int32_t num_wires, int32_t adjoint);
+/* applyOperation(vector...) :640-676: a list of operations, in order. */
+PLK_API int plk_apply_ops(plk_state s, const plk_op *ops, int32_t num_ops);
+/* applyGenerator :687-695: apply the generator of `gate`, return its scale
+ * factor (the value the reference's applyGenerator* returns). */
+PLK_API int plk_apply_generator(plk_state s, int32_t gate, const int64_t *wires, int32_t num_wires,
+                                int32_t adjoint, double *scale);
+
+/* ---- expectation values and linear algebra --------------------------- */
+/* getExpectationValue{Identity,PauliX,PauliY,PauliZ,Hadamard}
+ * (simulator/MeasuresKokkos.hpp:167-271, ExpValFunctors.hpp:13-153);
+ * gate must be one of IDENTITY, PAULIX, PAULIY, PAULIZ, HADAMARD. */
+PLK_API int plk_expval_named(plk_state s, int32_t gate, const int64_t *wires, int32_t num_wires,
+                             double *out);
+/* Several named one-wire expectation values in one pass over the state
+ * (count values; gates[i] on wires[i]). */
+PLK_API int plk_expval_named_batch(plk_state s, int32_t count, const int32_t *gates,
+                                   const int64_t *wires, double *out);
+/* getExpectationValueMultiQubitOp :318-346 (1q/2q functors :155-250; k >= 3
+ * matrices: Re<psi|M psi>). */
+PLK_API int plk_expval_matrix(plk_state s, const double *matrix, const int64_t *wires,
+                              int32_t num_wires, double *out);
+/* getExpectationValue(data, indices, index_ptr) :111-135,
+ * ExpValFunctors.hpp:252-280: CSR matrix (complex128 values). */
+PLK_API int plk_expval_sparse(plk_state s, const double *data, const int64_t *indices,
+                              const int64_t *indptr, int64_t num_rows, int64_t nnz, double *out);
+/* Expectation value of a sum of Pauli words sum_j c_j P_j (the Hamiltonian
+ * of NamedObs/TensorProdObs Pauli terms, ObservablesKokkos.hpp:296-402),
+ * without materialising O|psi>.  Term j acts on
+ * wires[offsets[j] .. offsets[j+1]) with letters paulis[offsets[j] ..]
+ * ('I', 'X', 'Y', 'Z'). */
+PLK_API int plk_expval_pauli_sum(plk_state s, int32_t num_terms, const double *coeffs,
+                                 const int64_t *offsets, const int64_t *wires, const char *paulis,
+                                 double *out);
+/* out = sum_j c_j P_j in  (materialised Hamiltonian application; out != in) */
+PLK_API int plk_apply_pauli_sum(plk_state out, plk_state in, int32_t num_terms, const double *coeffs,
+                                const int64_t *offsets, const int64_t *wires, const char *paulis);
+/* getRealOfComplexInnerProduct / getImagOfComplexInnerProduct
+ * (LinearAlgebraKokkos.hpp:155-236): <x|y> = sum conj(x_k) y_k. */
+PLK_API int plk_inner_product(plk_state x, plk_state y, double *re, double *im);
+/* SparseMV_Kokkos (LinearAlgebraKokkos.hpp:68-148): y = A x (CSR). */
+PLK_API int plk_spmv(plk_state y, plk_state x, const double *data, const int64_t *indices,
+                     const int64_t *indptr, int64_t num_rows, int64_t nnz);
+
+/* ---- probabilities and sampling -------------------------------------- */
+/* probs() :389-408 (num_wires == 0) and probs(wires) :418-517: marginal
+ * probabilities in the requested wire order, written to host `out`
+ * (2^num_wires doubles). */
+PLK_API int plk_probs(plk_state s, const int64_t *wires, int32_t num_wires, double *out);
+/* getCDFFunctor (MeasuresFunctors.hpp:39-56): exclusive prefix sum of |psi|^2
+ * in FP64, written to host `out` (2^n doubles). */
+PLK_API int plk_cdf(plk_state s, double *out);
+/* Sampler (MeasuresFunctors.hpp:86-119) with caller-supplied uniforms
+ * (host, `shots` doubles in [0,1)); writes shots x n bits, MSB first. */
+PLK_API int plk_sample_from_uniforms(plk_state s, const double *uniforms, uint64_t shots,
+                                     int64_t *out_bits);
+/* The same search over a caller-supplied CDF (host, `length` doubles):
+ * identical indices for identical CDF and uniforms. */
+PLK_API int plk_search_cdf(const double *cdf, uint64_t length, int32_t num_qubits,
+                           const double *uniforms, uint64_t shots, int64_t *out_bits,
+                           int device);
+/* generate_samples :530-569: uniforms from a counter-based generator
+ * (Philox-4x32-10) seeded by `seed`. */
+PLK_API int plk_generate_samples(plk_state s, uint64_t shots, uint64_t seed, int64_t *out_bits);
+
+/* ---- adjoint Jacobian ------------------------------------------------- */
+/* AdjointJacobianKokkos::adjointJacobian (AdjointDiffKokkos.hpp:404-478),
+ * apply_operations = false.  `lambda` is the forward-evolved state (not
+ * modified); hlambda[i] = O_i|lambda> (overwritten).  Ops with more than one
+ * parameter are rejected, StatePrep/BasisState are not representable here
+ * (the host layer drops them).  jac is [num_obs][num_trainable] row-major;
+ * trainable holds sorted indices into the parametric ops. */
+PLK_API int plk_adjoint_jacobian(plk_state lambda, plk_state *hlambda, int32_t num_obs,
+                                 const plk_op *ops, int32_t num_ops, const int64_t *trainable,
+                                 int32_t num_trainable, double *jac);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PLK_GB300_H */

@@ -1,0 +1,438 @@
+// adjoint.cu — adjoint-method Jacobian with a fused backward step.
+//
+// Restates AdjointJacobianKokkos::adjointJacobian
+// (algorithms/AdjointDiffKokkos.hpp:404-478, apply_operations = false):
+// walking the ops backwards, lambda <- U^dag lambda, and for a trainable op
+//   jac[o][t] = -2 * scale * Im <H_lambda_o | G lambda_old>
+// then H_lambda_o <- U^dag H_lambda_o.  The reference materialises
+// mu = G lambda_old with a state copy, a generator sweep and one host-synced
+// reduction per (op, observable): about (num_obs + 4) state sweeps per op.
+// Here one kernel per trainable op reads lambda and every H_lambda_o once,
+// applies the generator to a register copy, accumulates the imaginary inner
+// products in FP64 (deterministic block reduction), applies U^dag to both and
+// writes them back: 2 * (1 + num_obs) state passes per op, no host round trip
+// until the Jacobian is complete.  Observables are processed in chunks of up
+// to 8 per launch; lambda is written by the last chunk only.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "gate_ops.cuh"
+#include "reduce.cuh"
+
+namespace plk {
+
+int plan_gate(int gate, int nw, bool inv, const double *prm, int np, GatePlan &p);
+int plan_generator(int gate, int nw, GatePlan &p);
+int apply_gate_impl(plk_state s, int gate, const int64_t *wires, int nw, bool adj, const double *params, int np,
+                    const double *matrix);
+
+enum AdjKind : int {
+    A_RX = 0, A_RY, A_RZ, A_PS, A_CRX, A_CRY, A_CRZ, A_CPS, A_IXX, A_IXY, A_IYY, A_IZZ,
+    A_SE, A_SEM, A_SEP, A_DE, A_DEM, A_DEP, A_MRZ, A_NONE
+};
+
+static int adj_kind(int gate) {
+    switch (gate) {
+    case PLK_GATE_RX: return A_RX;
+    case PLK_GATE_RY: return A_RY;
+    case PLK_GATE_RZ: return A_RZ;
+    case PLK_GATE_PHASESHIFT: return A_PS;
+    case PLK_GATE_CRX: return A_CRX;
+    case PLK_GATE_CRY: return A_CRY;
+    case PLK_GATE_CRZ: return A_CRZ;
+    case PLK_GATE_CONTROLLEDPHASESHIFT: return A_CPS;
+    case PLK_GATE_ISINGXX: return A_IXX;
+    case PLK_GATE_ISINGXY: return A_IXY;
+    case PLK_GATE_ISINGYY: return A_IYY;
+    case PLK_GATE_ISINGZZ: return A_IZZ;
+    case PLK_GATE_SINGLEEXCITATION: return A_SE;
+    case PLK_GATE_SINGLEEXCITATIONMINUS: return A_SEM;
+    case PLK_GATE_SINGLEEXCITATIONPLUS: return A_SEP;
+    case PLK_GATE_DOUBLEEXCITATION: return A_DE;
+    case PLK_GATE_DOUBLEEXCITATIONMINUS: return A_DEM;
+    case PLK_GATE_DOUBLEEXCITATIONPLUS: return A_DEP;
+    case PLK_GATE_MULTIRZ: return A_MRZ;
+    default: return A_NONE;
+    }
+}
+
+template <int KIND> __host__ __device__ constexpr int adj_K() {
+    return KIND <= A_PS ? 1 : (KIND <= A_SEP ? 2 : (KIND <= A_DEP ? 4 : 0));
+}
+
+// Local indices where the gate or the generator acts.  Outside this set the
+// gate is the identity and G lambda vanishes, so neither the update nor the
+// inner product needs those amplitudes.
+template <int KIND> __host__ __device__ constexpr uint32_t adj_touch() {
+    switch (KIND) {
+    case A_RX: case A_RY: case A_RZ: return 0x3u;
+    case A_PS: return 0x2u;
+    case A_CRX: case A_CRY: case A_CRZ: return 0xCu;
+    case A_CPS: return 0x8u;
+    case A_IXX: case A_IYY: case A_IZZ: case A_SEM: case A_SEP: return 0xFu;
+    case A_IXY: case A_SE: return 0x6u;
+    case A_DE: return (1u << 3) | (1u << 12);
+    case A_DEM: case A_DEP: return 0xFFFFu;
+    default: return 0x1u;
+    }
+}
+
+template <class T> struct AdjArgs {
+    Masks mk;
+    uint64_t ngroups;
+    uint64_t off[16];
+    uint64_t mrz_mask;
+    T g[8];  // gate (U^dag) coefficients
+    T e[2];  // phase on the other amplitudes (+/- excitation gates)
+};
+
+// U^dag on the touched amplitudes (coefficients planned for adjoint = !inverse)
+template <int KIND, class V, class T> __device__ __forceinline__ void adj_gate(V *v, const AdjArgs<T> &a) {
+    if constexpr (KIND == A_RX) pair_op<P_RX>(v[0], v[1], a.g);
+    else if constexpr (KIND == A_RY) pair_op<P_RY>(v[0], v[1], a.g);
+    else if constexpr (KIND == A_RZ) pair_op<P_DIAG>(v[0], v[1], a.g);
+    else if constexpr (KIND == A_PS) pair_op<P_PHASE_Y>(v[0], v[1], a.g);
+    else if constexpr (KIND == A_CRX) pair_op<P_RX>(v[2], v[3], a.g);
+    else if constexpr (KIND == A_CRY) pair_op<P_RY>(v[2], v[3], a.g);
+    else if constexpr (KIND == A_CRZ) pair_op<P_DIAG>(v[2], v[3], a.g);
+    else if constexpr (KIND == A_CPS) pair_op<P_PHASE_Y>(v[2], v[3], a.g);
+    else if constexpr (KIND == A_IXX) {
+        V q[4] = {v[0], v[1], v[2], v[3]};
+        quad_op<Q_IXX>(q, a.g);
+        for (int i = 0; i < 4; i++) v[i] = q[i];
+    } else if constexpr (KIND == A_IYY) {
+        V q[4] = {v[0], v[1], v[2], v[3]};
+        quad_op<Q_IYY>(q, a.g);
+        for (int i = 0; i < 4; i++) v[i] = q[i];
+    } else if constexpr (KIND == A_IZZ) {
+        V q[4] = {v[0], v[1], v[2], v[3]};
+        quad_op<Q_DIAG>(q, a.g);
+        for (int i = 0; i < 4; i++) v[i] = q[i];
+    } else if constexpr (KIND == A_IXY) pair_op<P_RX>(v[1], v[2], a.g);
+    else if constexpr (KIND == A_SE) pair_op<P_RY>(v[1], v[2], a.g);
+    else if constexpr (KIND == A_SEM || KIND == A_SEP) {
+        pair_op<P_RY>(v[1], v[2], a.g);
+        v[0] = cmul(v[0], mk<V>(a.e[0], a.e[1]));
+        v[3] = cmul(v[3], mk<V>(a.e[0], a.e[1]));
+    } else if constexpr (KIND == A_DE) pair_op<P_RY>(v[3], v[12], a.g);
+    else if constexpr (KIND == A_DEM || KIND == A_DEP) {
+        pair_op<P_RY>(v[3], v[12], a.g);
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            if (i != 3 && i != 12) v[i] = cmul(v[i], mk<V>(a.e[0], a.e[1]));
+    }
+}
+
+// generator G on a copy (GateFunctors.hpp:2172-3132 and Pauli gates)
+template <int KIND, class V> __device__ __forceinline__ void adj_gen(V *v) {
+    const V Z = mk<V>(0, 0);
+    if constexpr (KIND == A_RX) {
+        V t = v[0]; v[0] = v[1]; v[1] = t;
+    } else if constexpr (KIND == A_RY) {
+        V t = v[0]; v[0] = mk<V>(v[1].y, -v[1].x); v[1] = mk<V>(-t.y, t.x);
+    } else if constexpr (KIND == A_RZ) {
+        v[1] = cneg(v[1]);
+    } else if constexpr (KIND == A_PS) {
+        v[0] = Z;
+    } else if constexpr (KIND == A_CRX) {
+        V t = v[2]; v[2] = v[3]; v[3] = t;
+    } else if constexpr (KIND == A_CRY) {
+        V t = v[2]; v[2] = mk<V>(v[3].y, -v[3].x); v[3] = mk<V>(-t.y, t.x);
+    } else if constexpr (KIND == A_CRZ) {
+        v[3] = cneg(v[3]);
+    } else if constexpr (KIND == A_CPS) {
+        // v[3] unchanged; v[0..2] are zero (outside the touched set)
+    } else if constexpr (KIND == A_IXX) {
+        V t = v[0]; v[0] = v[3]; v[3] = t;
+        t = v[1]; v[1] = v[2]; v[2] = t;
+    } else if constexpr (KIND == A_IYY) {
+        const V v00 = v[0];
+        v[0] = cneg(v[3]); v[3] = cneg(v00);
+        V t = v[1]; v[1] = v[2]; v[2] = t;
+    } else if constexpr (KIND == A_IZZ) {
+        v[1] = cneg(v[1]); v[2] = cneg(v[2]);
+    } else if constexpr (KIND == A_IXY) {
+        V t = v[1]; v[1] = v[2]; v[2] = t;
+    } else if constexpr (KIND == A_SE || KIND == A_SEM || KIND == A_SEP) {
+        V t = v[1];
+        v[1] = mk<V>(v[2].y, -v[2].x); // -i * old v10
+        v[2] = mk<V>(-t.y, t.x);       //  i * old v01
+        if constexpr (KIND == A_SEP) { v[0] = cneg(v[0]); v[3] = cneg(v[3]); }
+        if constexpr (KIND == A_SEM) { /* v[0], v[3] unchanged */ }
+    } else if constexpr (KIND == A_DE || KIND == A_DEM) {
+        V t = v[3];
+        v[3] = mk<V>(v[12].y, -v[12].x); // -i * v1100
+        v[12] = mk<V>(-t.y, t.x);        //  i * v0011
+    } else if constexpr (KIND == A_DEP) {
+        V t = v[3];
+        v[3] = mk<V>(-v[12].y, v[12].x); //  i * v1100
+        v[12] = mk<V>(t.y, -t.x);        // -i * v0011
+    }
+}
+
+constexpr int kAdjObsPerLaunch = 8;
+
+template <class T, int KIND, int NV>
+__global__ void __launch_bounds__(kThreads)
+    k_adj_fused(c2_t<T> *__restrict__ lam, c2_t<T> *const *__restrict__ hl, int nobs, int write_lambda,
+                const AdjArgs<T> a, double *partials, double *result, unsigned *counter, double post_scale) {
+    using V = c2_t<T>;
+    constexpr int K = adj_K<KIND>();
+    constexpr int D = 1 << K;
+    constexpr uint32_t TOUCH = adj_touch<KIND>();
+    double acc[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) acc[v] = 0.0;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.ngroups; g += step) {
+        uint64_t base;
+        V lv[D];
+        if constexpr (KIND == A_MRZ) {
+            base = g;
+            lv[0] = lam[g];
+        } else {
+            base = group_base<K>(g, a.mk);
+#pragma unroll
+            for (int i = 0; i < D; i++)
+                if (TOUCH & (1u << i)) lv[i] = lam[base + a.off[i]];
+        }
+        // mu = G lambda (register copy)
+        V mu[D];
+#pragma unroll
+        for (int i = 0; i < D; i++) mu[i] = lv[i];
+        if constexpr (KIND == A_MRZ) {
+            if (__popcll(g & a.mrz_mask) & 1) mu[0] = cneg(mu[0]);
+        } else {
+            adj_gen<KIND>(mu);
+        }
+#pragma unroll
+        for (int o = 0; o < NV; o++) {
+            if (o < nobs) {
+                V hv[D];
+                if constexpr (KIND == A_MRZ) {
+                    hv[0] = hl[o][g];
+                } else {
+#pragma unroll
+                    for (int i = 0; i < D; i++)
+                        if (TOUCH & (1u << i)) hv[i] = hl[o][base + a.off[i]];
+                }
+                double im = 0.0;
+#pragma unroll
+                for (int i = 0; i < D; i++)
+                    if (TOUCH & (1u << i)) im += (double)hv[i].x * mu[i].y - (double)hv[i].y * mu[i].x;
+                acc[o] += im;
+                if constexpr (KIND == A_MRZ) {
+                    const bool odd = __popcll(g & a.mrz_mask) & 1;
+                    hl[o][g] = odd ? cmul(hv[0], mk<V>(a.g[2], a.g[3])) : cmul(hv[0], mk<V>(a.g[0], a.g[1]));
+                } else {
+                    adj_gate<KIND>(hv, a);
+#pragma unroll
+                    for (int i = 0; i < D; i++)
+                        if (TOUCH & (1u << i)) hl[o][base + a.off[i]] = hv[i];
+                }
+            }
+        }
+        if (write_lambda) {
+            if constexpr (KIND == A_MRZ) {
+                const bool odd = __popcll(g & a.mrz_mask) & 1;
+                lam[g] = odd ? cmul(lv[0], mk<V>(a.g[2], a.g[3])) : cmul(lv[0], mk<V>(a.g[0], a.g[1]));
+            } else {
+                adj_gate<KIND>(lv, a);
+#pragma unroll
+                for (int i = 0; i < D; i++)
+                    if (TOUCH & (1u << i)) lam[base + a.off[i]] = lv[i];
+            }
+        }
+    }
+    block_reduce_finish<NV>(acc, partials, result, counter, post_scale, nobs);
+}
+
+template <class T, int KIND>
+static int launch_fused_kind(plk_state lam, c2_t<T> *const *d_hl, int nobs, int write_lambda, const AdjArgs<T> &a,
+                             double *result, double post_scale) {
+    const int grid = red_grid(lam, a.ngroups);
+    auto &w = lam->ws;
+    auto *lp = (c2_t<T> *)lam->data;
+    if (nobs <= 1)
+        k_adj_fused<T, KIND, 1><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials, result,
+                                                                   w.d_counter, post_scale);
+    else if (nobs <= 2)
+        k_adj_fused<T, KIND, 2><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials, result,
+                                                                   w.d_counter, post_scale);
+    else if (nobs <= 4)
+        k_adj_fused<T, KIND, 4><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials, result,
+                                                                   w.d_counter, post_scale);
+    else
+        k_adj_fused<T, KIND, 8><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials, result,
+                                                                   w.d_counter, post_scale);
+    PLK_CHECK_LAUNCH();
+    return PLK_OK;
+}
+
+template <class T>
+static int launch_fused(int kind, plk_state lam, c2_t<T> *const *d_hl, int nobs, int write_lambda, const AdjArgs<T> &a,
+                        double *result, double post_scale) {
+#define PLK_ADJ_CASE(K)                                                                                                \
+    case K: return launch_fused_kind<T, K>(lam, d_hl, nobs, write_lambda, a, result, post_scale);
+    switch (kind) {
+        PLK_ADJ_CASE(A_RX) PLK_ADJ_CASE(A_RY) PLK_ADJ_CASE(A_RZ) PLK_ADJ_CASE(A_PS) PLK_ADJ_CASE(A_CRX)
+        PLK_ADJ_CASE(A_CRY) PLK_ADJ_CASE(A_CRZ) PLK_ADJ_CASE(A_CPS) PLK_ADJ_CASE(A_IXX) PLK_ADJ_CASE(A_IXY)
+        PLK_ADJ_CASE(A_IYY) PLK_ADJ_CASE(A_IZZ) PLK_ADJ_CASE(A_SE) PLK_ADJ_CASE(A_SEM) PLK_ADJ_CASE(A_SEP)
+        PLK_ADJ_CASE(A_DE) PLK_ADJ_CASE(A_DEM) PLK_ADJ_CASE(A_DEP) PLK_ADJ_CASE(A_MRZ)
+    default: PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "internal: no fused adjoint kernel");
+    }
+#undef PLK_ADJ_CASE
+}
+
+// One trainable backward step for all observables.
+template <class T>
+static int fused_step(plk_state lam, c2_t<T> *const *d_hl, int nobs, const plk_op &op, double scale, double *d_jac_col) {
+    const int kind = adj_kind(op.gate);
+    if (kind == A_NONE) PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "no generator for this gate");
+    GatePlan p;
+    PLK_TRY(plan_gate(op.gate, op.num_wires, op.adjoint == 0, op.params, op.num_params, p)); // U^dag
+    AdjArgs<T> a;
+    std::memset(&a, 0, sizeof(a));
+    for (int j = 0; j < 8; j++) a.g[j] = (T)p.coef[j];
+    a.e[0] = (T)p.extra_e[0];
+    a.e[1] = (T)p.extra_e[1];
+    if (kind == A_MRZ) {
+        a.ngroups = lam->length;
+        for (int j = 0; j < op.num_wires; j++) a.mrz_mask |= 1ULL << (lam->nq - 1 - op.wires[j]);
+    } else {
+        const int K = op.num_wires;
+        int rev[4], srt[4];
+        for (int j = 0; j < K; j++) rev[j] = lam->nq - 1 - (int)op.wires[j];
+        std::copy(rev, rev + K, srt);
+        std::sort(srt, srt + K);
+        a.mk = make_masks(srt, K);
+        a.ngroups = lam->length >> K;
+        for (int i = 0; i < (1 << K); i++) {
+            uint64_t o = 0;
+            for (int j = 0; j < K; j++)
+                if ((i >> (K - 1 - j)) & 1) o |= 1ULL << rev[j];
+            a.off[i] = o;
+        }
+    }
+    if (nobs == 0) {
+        // nothing to differentiate against: just advance lambda
+        return apply_gate_impl(lam, op.gate, op.wires, op.num_wires, op.adjoint == 0, op.params, op.num_params, nullptr);
+    }
+    for (int o0 = 0; o0 < nobs; o0 += kAdjObsPerLaunch) {
+        const int nv = std::min(kAdjObsPerLaunch, nobs - o0);
+        const int last = (o0 + nv == nobs);
+        PLK_TRY(launch_fused<T>(kind, lam, d_hl + o0, nv, last, a, d_jac_col + o0, -2.0 * scale));
+    }
+    return PLK_OK;
+}
+
+template <class T>
+static int adjoint_impl(plk_state lam, plk_state *hl, int nobs, const plk_op *ops, int nops, const int64_t *tp,
+                        int ntp, double *jac) {
+    using V = c2_t<T>;
+    // device pointer table of the H_lambda states
+    std::vector<V *> hp(std::max(nobs, 1));
+    for (int o = 0; o < nobs; o++) hp[o] = (V *)hl[o]->data;
+    V **d_hl = nullptr;
+    double *d_jac = nullptr; // [ntp][nobs]
+    PLK_CUDA(cudaMallocAsync((void **)&d_hl, sizeof(V *) * hp.size(), lam->stream));
+    PLK_CUDA(cudaMemcpyAsync(d_hl, hp.data(), sizeof(V *) * hp.size(), cudaMemcpyHostToDevice, lam->stream));
+    PLK_CUDA(cudaMallocAsync((void **)&d_jac, sizeof(double) * std::max(1, ntp * nobs), lam->stream));
+    PLK_CUDA(cudaMemsetAsync(d_jac, 0, sizeof(double) * std::max(1, ntp * nobs), lam->stream));
+
+    int num_param_ops = 0;
+    for (int i = 0; i < nops; i++)
+        if (ops[i].num_params > 0) num_param_ops++;
+    int tp_number = ntp - 1;
+    long current_param_idx = num_param_ops - 1;
+    int tp_it = ntp - 1;
+    int st = PLK_OK;
+    for (int i = nops - 1; i >= 0 && st == PLK_OK; i--) {
+        const plk_op &op = ops[i];
+        if (op.num_params > 1) {
+            set_error("The operation is not supported using the adjoint differentiation method");
+            st = PLK_ERR_INVALID_ARG;
+            break;
+        }
+        if (tp_it < 0) break; // all trainable parameters done
+        const bool trainable = op.num_params > 0 && current_param_idx == tp[tp_it];
+        if (trainable) {
+            GatePlan gp;
+            st = plan_generator(op.gate, op.num_wires, gp);
+            if (st != PLK_OK) break;
+            const double scale = gp.scale * (op.adjoint ? -1.0 : 1.0);
+            st = fused_step<T>(lam, d_hl, nobs, op, scale, d_jac + (size_t)tp_number * nobs);
+            tp_number--;
+            tp_it--;
+        } else {
+            const bool adj = op.adjoint == 0;
+            st = apply_gate_impl(lam, op.gate, op.wires, op.num_wires, adj, op.params, op.num_params, op.matrix);
+            for (int o = 0; o < nobs && st == PLK_OK; o++)
+                st = apply_gate_impl(hl[o], op.gate, op.wires, op.num_wires, adj, op.params, op.num_params, op.matrix);
+        }
+        if (op.num_params > 0) current_param_idx--;
+    }
+    std::vector<double> hj((size_t)std::max(1, ntp * nobs));
+    if (st == PLK_OK && ntp * nobs > 0) {
+        PLK_CUDA(cudaMemcpyAsync(hj.data(), d_jac, sizeof(double) * ntp * nobs, cudaMemcpyDeviceToHost, lam->stream));
+    }
+    cudaFreeAsync(d_hl, lam->stream);
+    cudaFreeAsync(d_jac, lam->stream);
+    PLK_CUDA(cudaStreamSynchronize(lam->stream));
+    if (st != PLK_OK) return st;
+    for (int t = 0; t < ntp; t++)
+        for (int o = 0; o < nobs; o++) jac[(size_t)o * ntp + t] = hj[(size_t)t * nobs + o];
+    return PLK_OK;
+}
+
+} // namespace plk
+
+using namespace plk;
+
+extern "C" {
+
+PLK_API int plk_adjoint_jacobian(plk_state lambda, plk_state *hlambda, int32_t nobs, const plk_op *ops, int32_t nops,
+                                 const int64_t *trainable, int32_t ntp, double *jac) {
+    PLK_TRY(check_state(lambda));
+    if (ntp <= 0) PLK_FAIL(PLK_ERR_INVALID_ARG, "No trainable parameters provided.");
+    if (!trainable || !jac || (nops > 0 && !ops) || nobs < 0 || (nobs > 0 && !hlambda))
+        PLK_FAIL(PLK_ERR_INVALID_ARG, "null argument");
+    for (int t = 1; t < ntp; t++)
+        if (trainable[t] <= trainable[t - 1]) PLK_FAIL(PLK_ERR_INVALID_ARG, "trainable parameters must be sorted and unique");
+    for (int o = 0; o < nobs; o++) {
+        PLK_TRY(check_state(hlambda[o]));
+        if (hlambda[o]->nq != lambda->nq || hlambda[o]->dtype != lambda->dtype)
+            PLK_FAIL(PLK_ERR_INVALID_ARG, "observable states differ in size or precision");
+        if (hlambda[o] == lambda) PLK_FAIL(PLK_ERR_INVALID_ARG, "lambda cannot be one of the observable states");
+        for (int p = 0; p < o; p++)
+            if (hlambda[p] == hlambda[o]) PLK_FAIL(PLK_ERR_INVALID_ARG, "repeated observable state");
+    }
+    for (int i = 0; i < nops; i++) {
+        const plk_op &op = ops[i];
+        if (op.gate < 0 || op.gate >= PLK_GATE_COUNT) PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "unknown gate in op list");
+        PLK_TRY(check_wires(lambda, op.wires, op.num_wires));
+    }
+    PLK_CUDA(cudaSetDevice(lambda->device));
+    // work copy of lambda, on lambda's stream; observable states join that stream
+    plk_state work = nullptr;
+    PLK_TRY(plk_state_create(lambda->nq, lambda->dtype, lambda->device, &work));
+    int st = plk_state_set_stream(work, lambda->stream);
+    if (st == PLK_OK) st = plk_state_copy(work, lambda);
+    std::vector<cudaStream_t> old_streams(nobs);
+    for (int o = 0; o < nobs && st == PLK_OK; o++) {
+        old_streams[o] = hlambda[o]->stream;
+        st = plk_state_set_stream(hlambda[o], lambda->stream);
+    }
+    if (st == PLK_OK)
+        st = lambda->dtype == PLK_C64 ? adjoint_impl<float>(work, hlambda, nobs, ops, nops, trainable, ntp, jac)
+                                      : adjoint_impl<double>(work, hlambda, nobs, ops, nops, trainable, ntp, jac);
+    const std::string err = st == PLK_OK ? std::string() : last_error();
+    for (int o = 0; o < nobs; o++)
+        if (old_streams[o]) plk_state_set_stream(hlambda[o], old_streams[o]);
+    plk_state_destroy(work);
+    if (st != PLK_OK) set_error(err);
+    return st;
+}
+
+} // extern "C"

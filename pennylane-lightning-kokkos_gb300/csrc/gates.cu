@@ -1,0 +1,692 @@
+// gates.cu — gate, matrix and generator kernels.
+//
+// Replaces the gate functors of simulator/GateFunctors.hpp and their
+// dispatch in simulator/StateVectorKokkos.hpp (applyOperation :585-676,
+// applySingle/Two/MultiQubitOp :704-796, applyGateFunctor :807-824,
+// applyMultiRZ :1222-1240, applyGenerator* :1275-1580).
+//
+// One kernel per local-operation shape instead of one functor per gate:
+//   k_pair  — grid-stride over groups, loads only the two amplitudes the
+//             gate changes (plus, for the +/- excitation gates and some
+//             generators, the other amplitudes of the group), vectorised
+//             float2/double2 loads;
+//   k_quad  — the four amplitudes of a two-wire group;
+//   k_mrz   — element-wise parity phase (MultiRZ and its generator);
+//   k_dense — 2^k x 2^k matrices for k >= 3, group vectors staged in shared
+//             memory, matrix in shared memory when it fits.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gate_ops.cuh"
+
+namespace plk {
+
+// ------------------------------------------------------------ gate table --
+struct GateInfo {
+    const char *name;
+    int nwires; // -1: any
+    int nparams;
+};
+
+static const GateInfo kGates[PLK_GATE_COUNT] = {
+    {"Identity", -1, 0},
+    {"PauliX", 1, 0}, {"PauliY", 1, 0}, {"PauliZ", 1, 0}, {"Hadamard", 1, 0},
+    {"S", 1, 0}, {"T", 1, 0}, {"PhaseShift", 1, 1}, {"RX", 1, 1}, {"RY", 1, 1},
+    {"RZ", 1, 1}, {"Rot", 1, 3},
+    {"CNOT", 2, 0}, {"CY", 2, 0}, {"CZ", 2, 0}, {"SWAP", 2, 0},
+    {"ControlledPhaseShift", 2, 1}, {"CRX", 2, 1}, {"CRY", 2, 1}, {"CRZ", 2, 1},
+    {"CRot", 2, 3}, {"IsingXX", 2, 1}, {"IsingXY", 2, 1}, {"IsingYY", 2, 1},
+    {"IsingZZ", 2, 1}, {"SingleExcitation", 2, 1},
+    {"SingleExcitationMinus", 2, 1}, {"SingleExcitationPlus", 2, 1},
+    {"DoubleExcitation", 4, 1}, {"DoubleExcitationMinus", 4, 1},
+    {"DoubleExcitationPlus", 4, 1}, {"CSWAP", 3, 0}, {"Toffoli", 3, 0},
+    {"MultiRZ", -1, 1},
+    {"Matrix", -1, 0},
+};
+
+// Rot = RZ(omega) RY(theta) RZ(phi) (rotFunctor GateFunctors.hpp:3134-3160);
+// the inverse negates and reverses the angles.
+static void rot_matrix(const double *p, bool inv, double *m) {
+    const double phi = inv ? -p[2] : p[0];
+    const double theta = inv ? -p[1] : p[1];
+    const double omega = inv ? -p[0] : p[2];
+    const double c = std::cos(theta / 2), s = std::sin(theta / 2);
+    const double pp = phi + omega, mm = phi - omega;
+    m[0] = std::cos(pp / 2) * c;  m[1] = -std::sin(pp / 2) * c;   // e^{-i p/2} c
+    m[2] = -std::cos(mm / 2) * s; m[3] = -std::sin(mm / 2) * s;   // -e^{i m/2} s
+    m[4] = std::cos(mm / 2) * s;  m[5] = -std::sin(mm / 2) * s;   // e^{-i m/2} s
+    m[6] = std::cos(pp / 2) * c;  m[7] = std::sin(pp / 2) * c;    // e^{i p/2} c
+}
+
+static void set_pair(GatePlan &p, int K, int op, int a, int b) {
+    p.family = GatePlan::F_PAIR;
+    p.K = K;
+    p.op = op;
+    p.a = a;
+    p.b = b;
+    p.n_extra = 0;
+    p.extra_mode = X_NONE;
+}
+
+static void set_extras(GatePlan &p, int mode, double er = 0, double ei = 0) {
+    const int dim = 1 << p.K;
+    p.n_extra = 0;
+    for (int i = 0; i < dim; i++)
+        if (i != p.a && i != p.b) p.extra_idx[p.n_extra++] = i;
+    p.extra_mode = mode;
+    p.extra_e[0] = er;
+    p.extra_e[1] = ei;
+}
+
+static void set_extras_list(GatePlan &p, int mode, std::initializer_list<int> idx) {
+    p.n_extra = 0;
+    for (int i : idx) p.extra_idx[p.n_extra++] = i;
+    p.extra_mode = mode;
+    p.extra_e[0] = p.extra_e[1] = 0;
+}
+
+// Plan of a named gate (GateFunctors.hpp functor constructors).
+int plan_gate(int gate, int nw, bool inv, const double *prm, int np, GatePlan &p) {
+    if (gate < 0 || gate >= PLK_GATE_COUNT || gate == PLK_GATE_MATRIX)
+        PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "unknown gate id " + std::to_string(gate));
+    const GateInfo &gi = kGates[gate];
+    if (gi.nwires > 0 && nw != gi.nwires)
+        PLK_FAIL(PLK_ERR_INVALID_ARG, std::string(gi.name) + " acts on " + std::to_string(gi.nwires) + " wires, got " +
+                                          std::to_string(nw));
+    if (np < gi.nparams)
+        PLK_FAIL(PLK_ERR_INVALID_ARG, std::string(gi.name) + " needs " + std::to_string(gi.nparams) + " parameter(s)");
+    if (gate == PLK_GATE_MULTIRZ && nw < 1) PLK_FAIL(PLK_ERR_INVALID_ARG, "MultiRZ needs at least one wire");
+    std::memset(p.coef, 0, sizeof(p.coef));
+    const double th = np > 0 ? prm[0] : 0.0;
+    const double ch = std::cos(th / 2), sh = std::sin(th / 2);
+    switch (gate) {
+    case PLK_GATE_IDENTITY: p.family = GatePlan::F_NOOP; return PLK_OK;
+    case PLK_GATE_PAULIX: set_pair(p, 1, P_SWAP, 0, 1); break;
+    case PLK_GATE_PAULIY: set_pair(p, 1, P_Y, 0, 1); break;
+    case PLK_GATE_PAULIZ: set_pair(p, 1, P_PHASE_Y, 0, 1); p.coef[0] = -1; break;
+    case PLK_GATE_HADAMARD: set_pair(p, 1, P_H, 0, 1); break;
+    case PLK_GATE_S: set_pair(p, 1, P_PHASE_Y, 0, 1); p.coef[0] = 0; p.coef[1] = inv ? -1 : 1; break;
+    case PLK_GATE_T:
+        set_pair(p, 1, P_PHASE_Y, 0, 1);
+        p.coef[0] = std::cos(M_PI / 4);
+        p.coef[1] = inv ? -std::sin(M_PI / 4) : std::sin(M_PI / 4);
+        break;
+    case PLK_GATE_PHASESHIFT:
+        set_pair(p, 1, P_PHASE_Y, 0, 1);
+        p.coef[0] = std::cos(th);
+        p.coef[1] = inv ? -std::sin(th) : std::sin(th);
+        break;
+    case PLK_GATE_RX: // rxFunctor: s = inverse ? sin(t/2) : sin(-t/2)
+        set_pair(p, 1, P_RX, 0, 1);
+        p.coef[0] = std::cos(th * 0.5);
+        p.coef[1] = inv ? std::sin(th * 0.5) : std::sin(-th * 0.5);
+        break;
+    case PLK_GATE_RY: // ryFunctor: s = inverse ? -sin(t/2) : sin(t/2)
+        set_pair(p, 1, P_RY, 0, 1);
+        p.coef[0] = std::cos(th * 0.5);
+        p.coef[1] = inv ? -std::sin(th * 0.5) : std::sin(th * 0.5);
+        break;
+    case PLK_GATE_RZ: // rzFunctor: (c, -s), (c, s); inverse conjugates
+        set_pair(p, 1, P_DIAG, 0, 1);
+        p.coef[0] = ch; p.coef[1] = inv ? sh : -sh;
+        p.coef[2] = ch; p.coef[3] = inv ? -sh : sh;
+        break;
+    case PLK_GATE_ROT: set_pair(p, 1, P_MAT, 0, 1); rot_matrix(prm, inv, p.coef); break;
+    // two-wire gates: local index bit 1 = wires[0] (control), bit 0 = wires[1]
+    case PLK_GATE_CNOT: set_pair(p, 2, P_SWAP, 2, 3); break;
+    case PLK_GATE_CY: set_pair(p, 2, P_Y, 2, 3); break;
+    case PLK_GATE_CZ: set_pair(p, 2, P_PHASE_Y, 2, 3); p.coef[0] = -1; break;
+    case PLK_GATE_SWAP: set_pair(p, 2, P_SWAP, 1, 2); break;
+    case PLK_GATE_CONTROLLEDPHASESHIFT:
+        set_pair(p, 2, P_PHASE_Y, 2, 3);
+        p.coef[0] = std::cos(th);
+        p.coef[1] = inv ? -std::sin(th) : std::sin(th);
+        break;
+    case PLK_GATE_CRX: // crxFunctor: js = inverse ? -sin : sin, same rotation as RX with s = -js
+        set_pair(p, 2, P_RX, 2, 3);
+        p.coef[0] = ch;
+        p.coef[1] = inv ? sh : -sh;
+        break;
+    case PLK_GATE_CRY:
+        set_pair(p, 2, P_RY, 2, 3);
+        p.coef[0] = ch;
+        p.coef[1] = inv ? -sh : sh;
+        break;
+    case PLK_GATE_CRZ:
+        set_pair(p, 2, P_DIAG, 2, 3);
+        p.coef[0] = ch; p.coef[1] = inv ? sh : -sh;
+        p.coef[2] = ch; p.coef[3] = inv ? -sh : sh;
+        break;
+    case PLK_GATE_CROT: set_pair(p, 2, P_MAT, 2, 3); rot_matrix(prm, inv, p.coef); break;
+    case PLK_GATE_ISINGXX:
+        p.family = GatePlan::F_QUAD; p.K = 2; p.op = Q_IXX;
+        p.coef[0] = ch; p.coef[1] = inv ? -sh : sh;
+        break;
+    case PLK_GATE_ISINGXY: // isingXYFunctor leaves |00>, |11>; rotates (01, 10) like RX with s = sj
+        set_pair(p, 2, P_RX, 1, 2);
+        p.coef[0] = ch; p.coef[1] = inv ? -sh : sh;
+        break;
+    case PLK_GATE_ISINGYY:
+        p.family = GatePlan::F_QUAD; p.K = 2; p.op = Q_IYY;
+        p.coef[0] = ch; p.coef[1] = inv ? -sh : sh;
+        break;
+    case PLK_GATE_ISINGZZ: {
+        p.family = GatePlan::F_QUAD; p.K = 2; p.op = Q_DIAG;
+        const double s0i = inv ? sh : -sh, s1i = inv ? -sh : sh;
+        const double d[8] = {ch, s0i, ch, s1i, ch, s1i, ch, s0i};
+        std::memcpy(p.coef, d, sizeof(d));
+        break;
+    }
+    case PLK_GATE_SINGLEEXCITATION:
+        set_pair(p, 2, P_RY, 1, 2);
+        p.coef[0] = ch; p.coef[1] = inv ? -sh : sh;
+        break;
+    case PLK_GATE_SINGLEEXCITATIONMINUS:
+    case PLK_GATE_SINGLEEXCITATIONPLUS: {
+        set_pair(p, 2, P_RY, 1, 2);
+        p.coef[0] = ch; p.coef[1] = inv ? -sh : sh;
+        // SE-: e = inverse ? e^{i t/2} : e^{-i t/2};  SE+: the opposite
+        const bool minus = gate == PLK_GATE_SINGLEEXCITATIONMINUS;
+        const double si = (minus != inv) ? -sh : sh;
+        set_extras(p, X_PHASE, ch, si);
+        break;
+    }
+    case PLK_GATE_DOUBLEEXCITATION:
+        set_pair(p, 4, P_RY, 3, 12);
+        p.coef[0] = ch; p.coef[1] = inv ? -sh : sh;
+        break;
+    case PLK_GATE_DOUBLEEXCITATIONMINUS:
+    case PLK_GATE_DOUBLEEXCITATIONPLUS: {
+        set_pair(p, 4, P_RY, 3, 12);
+        p.coef[0] = ch; p.coef[1] = inv ? -sh : sh;
+        const bool minus = gate == PLK_GATE_DOUBLEEXCITATIONMINUS;
+        const double si = (minus != inv) ? -sh : sh;
+        set_extras(p, X_PHASE, ch, si);
+        break;
+    }
+    case PLK_GATE_CSWAP: set_pair(p, 3, P_SWAP, 5, 6); break;
+    case PLK_GATE_TOFFOLI: set_pair(p, 3, P_SWAP, 7, 6); break;
+    case PLK_GATE_MULTIRZ:
+        p.family = GatePlan::F_MRZ; p.K = nw;
+        p.coef[0] = ch; p.coef[1] = inv ? sh : -sh; // shift_0 (even parity)
+        p.coef[2] = ch; p.coef[3] = inv ? -sh : sh; // shift_1 (odd parity)
+        break;
+    default: PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "unknown gate id " + std::to_string(gate));
+    }
+    return PLK_OK;
+}
+
+// Plan of a generator (applyGenerator*, StateVectorKokkos.hpp:1275-1580 and
+// the generator functors GateFunctors.hpp:2172-3132); the adjoint flag is
+// ignored, as the reference's generator functors ignore it.
+int plan_generator(int gate, int nw, GatePlan &p) {
+    if (gate < 0 || gate >= PLK_GATE_COUNT) PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "unknown gate id");
+    const GateInfo &gi = kGates[gate];
+    if (gi.nwires > 0 && nw != gi.nwires)
+        PLK_FAIL(PLK_ERR_INVALID_ARG, std::string(gi.name) + " acts on " + std::to_string(gi.nwires) + " wires");
+    std::memset(p.coef, 0, sizeof(p.coef));
+    p.scale = -0.5;
+    switch (gate) {
+    case PLK_GATE_RX: set_pair(p, 1, P_SWAP, 0, 1); break;
+    case PLK_GATE_RY: set_pair(p, 1, P_Y, 0, 1); break;
+    case PLK_GATE_RZ: set_pair(p, 1, P_PHASE_Y, 0, 1); p.coef[0] = -1; break;
+    case PLK_GATE_PHASESHIFT: set_pair(p, 1, P_ZERO_Y, 1, 0); p.scale = 1.0; break;
+    case PLK_GATE_CONTROLLEDPHASESHIFT:
+        set_pair(p, 2, P_ZERO, 0, 1);
+        set_extras_list(p, X_ZERO, {2});
+        p.scale = 1.0;
+        break;
+    case PLK_GATE_CRX: set_pair(p, 2, P_SWAP, 2, 3); set_extras_list(p, X_ZERO, {0, 1}); break;
+    case PLK_GATE_CRY: set_pair(p, 2, P_Y, 2, 3); set_extras_list(p, X_ZERO, {0, 1}); break;
+    case PLK_GATE_CRZ:
+        set_pair(p, 2, P_PHASE_Y, 2, 3);
+        p.coef[0] = -1;
+        set_extras_list(p, X_ZERO, {0, 1});
+        break;
+    case PLK_GATE_ISINGXX: p.family = GatePlan::F_QUAD; p.K = 2; p.op = Q_GEN_IXX; break;
+    case PLK_GATE_ISINGXY:
+        set_pair(p, 2, P_SWAP, 1, 2);
+        set_extras_list(p, X_ZERO, {0, 3});
+        p.scale = 0.5;
+        break;
+    case PLK_GATE_ISINGYY: p.family = GatePlan::F_QUAD; p.K = 2; p.op = Q_GEN_IYY; break;
+    case PLK_GATE_ISINGZZ:
+        set_pair(p, 2, P_DIAG, 1, 2);
+        p.coef[0] = -1; p.coef[2] = -1;
+        break;
+    case PLK_GATE_SINGLEEXCITATION:
+        set_pair(p, 2, P_GEN_SWAPI, 1, 2);
+        p.coef[0] = 1;
+        set_extras_list(p, X_ZERO, {0, 3});
+        break;
+    case PLK_GATE_SINGLEEXCITATIONMINUS: set_pair(p, 2, P_GEN_SWAPI, 1, 2); p.coef[0] = 1; break;
+    case PLK_GATE_SINGLEEXCITATIONPLUS:
+        set_pair(p, 2, P_GEN_SWAPI, 1, 2);
+        p.coef[0] = 1;
+        set_extras_list(p, X_PHASE, {0, 3});
+        p.extra_e[0] = -1;
+        p.extra_e[1] = 0;
+        break;
+    case PLK_GATE_DOUBLEEXCITATION:
+        set_pair(p, 4, P_GEN_SWAPI, 3, 12);
+        p.coef[0] = 1;
+        set_extras(p, X_ZERO);
+        break;
+    case PLK_GATE_DOUBLEEXCITATIONMINUS: set_pair(p, 4, P_GEN_SWAPI, 3, 12); p.coef[0] = 1; break;
+    case PLK_GATE_DOUBLEEXCITATIONPLUS:
+        set_pair(p, 4, P_GEN_SWAPI, 3, 12);
+        p.coef[0] = -1;
+        p.scale = 0.5;
+        break;
+    case PLK_GATE_MULTIRZ:
+        if (nw < 1) PLK_FAIL(PLK_ERR_INVALID_ARG, "MultiRZ needs at least one wire");
+        p.family = GatePlan::F_GEN_MRZ;
+        p.K = nw;
+        break;
+    default:
+        PLK_FAIL(PLK_ERR_UNKNOWN_GATE, std::string("Generator does not exist for ") + gi.name);
+    }
+    return PLK_OK;
+}
+
+// Sorted bit positions, masks and local offsets of a wire list.
+struct WireGeom {
+    int K;
+    int rev[kMaxDenseWires];
+    int sorted[kMaxDenseWires];
+    Masks mk;
+    uint64_t local_off(int i) const { // local index bit (K-1-j) <-> wires[j]
+        uint64_t o = 0;
+        for (int j = 0; j < K; j++)
+            if ((i >> (K - 1 - j)) & 1) o |= 1ULL << rev[j];
+        return o;
+    }
+};
+
+static void wire_geom(int nq, const int64_t *wires, int K, WireGeom &g) {
+    g.K = K;
+    for (int j = 0; j < K; j++) g.rev[j] = nq - 1 - (int)wires[j];
+    std::copy(g.rev, g.rev + K, g.sorted);
+    std::sort(g.sorted, g.sorted + K);
+    g.mk = make_masks(g.sorted, K);
+}
+
+// ---------------------------------------------------------------- kernels --
+constexpr int kUnroll = 2;
+
+template <class T, int OP, int K>
+__global__ void __launch_bounds__(kThreads) k_pair(c2_t<T> *__restrict__ sv, const PairArgs<T> a) {
+    using V = c2_t<T>;
+    constexpr bool TX = pair_touches_x<OP>();
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x * kUnroll;
+    for (uint64_t g0 = (uint64_t)blockIdx.x * blockDim.x * kUnroll + threadIdx.x; g0 < a.ngroups; g0 += step) {
+        uint64_t base[kUnroll];
+        V x[kUnroll], y[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; u++) {
+            const uint64_t g = g0 + (uint64_t)u * blockDim.x;
+            base[u] = group_base<K>(g < a.ngroups ? g : 0, a.mk);
+            if (g < a.ngroups) {
+                if (TX) x[u] = sv[base[u] + a.offA];
+                y[u] = sv[base[u] + a.offB];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; u++) {
+            const uint64_t g = g0 + (uint64_t)u * blockDim.x;
+            if (g < a.ngroups) {
+                pair_op<OP>(x[u], y[u], a.coef);
+                if (TX) sv[base[u] + a.offA] = x[u];
+                sv[base[u] + a.offB] = y[u];
+                for (int j = 0; j < a.n_extra; j++) {
+                    V *p = sv + base[u] + a.off_extra[j];
+                    if (a.extra_mode == X_PHASE) *p = cmul(*p, mk<V>(a.e[0], a.e[1]));
+                    else *p = mk<V>(0, 0);
+                }
+            }
+        }
+    }
+}
+
+template <class T, int OP>
+__global__ void __launch_bounds__(kThreads) k_quad(c2_t<T> *__restrict__ sv, const QuadArgs<T> a) {
+    using V = c2_t<T>;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.ngroups; g += step) {
+        const uint64_t base = group_base<2>(g, a.mk);
+        V v[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) v[i] = sv[base + a.off[i]];
+        quad_op<OP>(v, a.coef);
+#pragma unroll
+        for (int i = 0; i < 4; i++) sv[base + a.off[i]] = v[i];
+    }
+}
+
+template <class T, bool GEN>
+__global__ void __launch_bounds__(kThreads) k_mrz(c2_t<T> *__restrict__ sv, uint64_t n, uint64_t mask, T e0r, T e0i,
+                                                   T e1r, T e1i) {
+    using V = c2_t<T>;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
+        const bool odd = __popcll(k & mask) & 1;
+        V v = sv[k];
+        if (GEN) {
+            if (odd) v = cneg(v);
+        } else {
+            v = odd ? cmul(v, mk<V>(e1r, e1i)) : cmul(v, mk<V>(e0r, e0i));
+        }
+        sv[k] = v;
+    }
+}
+
+// Dense 2^k x 2^k matrix, k >= 3.  Rows r of `ngrp` groups are handled by one
+// thread each; the group vectors are staged in shared memory, the matrix sits
+// in shared memory when it fits (k <= kSmemMatWires) and is read through L2
+// otherwise.
+constexpr int kSmemMatWires = 5;
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_dense(c2_t<T> *__restrict__ sv, const c2_t<T> *__restrict__ mat,
+                                                     const uint64_t *__restrict__ off, Masks gm, int K,
+                                                     uint64_t ngroups, int mat_in_smem) {
+    using V = c2_t<T>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int dim = 1 << K;
+    V *smat = reinterpret_cast<V *>(smem_raw);
+    V *svec = smat + (mat_in_smem ? dim * dim : 0);
+    if (mat_in_smem)
+        for (int i = threadIdx.x; i < dim * dim; i += blockDim.x) smat[i] = mat[i];
+    const V *M = mat_in_smem ? smat : mat;
+    const int gpb = dim >= kThreads ? 1 : kThreads / dim; // groups per block iteration
+    const int rows_per_thread = dim >= kThreads ? dim / kThreads : 1;
+    for (uint64_t gb = (uint64_t)blockIdx.x * gpb; gb < ngroups; gb += (uint64_t)gridDim.x * gpb) {
+        __syncthreads();
+        // stage group vectors
+        for (int t = threadIdx.x; t < gpb * dim; t += blockDim.x) {
+            const int gi = t / dim, r = t % dim;
+            const uint64_t g = gb + gi;
+            if (g < ngroups) {
+                uint64_t base = g & gm.m[0];
+                for (int j = 1; j <= K; j++) base |= (g << j) & gm.m[j];
+                svec[t] = sv[base + off[r]];
+            }
+        }
+        __syncthreads();
+        for (int rr = 0; rr < rows_per_thread; rr++) {
+            const int t = threadIdx.x + rr * kThreads;
+            const int gi = t / dim, r = t % dim;
+            const uint64_t g = gb + gi;
+            if (gi < gpb && g < ngroups) {
+                const V *vec = svec + gi * dim;
+                const V *row = M + (size_t)r * dim;
+                T ar = 0, ai = 0;
+                for (int j = 0; j < dim; j++) {
+                    const V m = row[j], v = vec[j];
+                    ar += m.x * v.x - m.y * v.y;
+                    ai += m.x * v.y + m.y * v.x;
+                }
+                uint64_t base = g & gm.m[0];
+                for (int j = 1; j <= K; j++) base |= (g << j) & gm.m[j];
+                sv[base + off[r]] = mk<V>(ar, ai);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------- launchers --
+template <class T> static int gate_grid(plk_state s, uint64_t work, int unroll) {
+    DeviceCtx *d = nullptr;
+    PLK_TRY(device_ctx(s->device, &d));
+    const uint64_t per_block = (uint64_t)kThreads * unroll;
+    uint64_t want = (work + per_block - 1) / per_block;
+    const uint64_t cap = (uint64_t)d->sm_count * (d->max_threads_per_sm / kThreads) * 8;
+    return (int)std::max<uint64_t>(1, std::min(want, cap));
+}
+
+template <class T, int OP>
+static void launch_pair_op(plk_state s, int K, int grid, const PairArgs<T> &a) {
+    auto *sv = (c2_t<T> *)s->data;
+    switch (K) {
+    case 1: k_pair<T, OP, 1><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case 2: k_pair<T, OP, 2><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case 3: k_pair<T, OP, 3><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    default: k_pair<T, OP, 4><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    }
+}
+
+template <class T> static int run_pair(plk_state s, const GatePlan &p, const WireGeom &g) {
+    PairArgs<T> a;
+    a.mk = g.mk;
+    a.ngroups = s->length >> p.K;
+    a.offA = g.local_off(p.a);
+    a.offB = g.local_off(p.b);
+    a.n_extra = p.n_extra;
+    a.extra_mode = p.extra_mode;
+    for (int j = 0; j < p.n_extra; j++) a.off_extra[j] = g.local_off(p.extra_idx[j]);
+    for (int j = 0; j < 8; j++) a.coef[j] = (T)p.coef[j];
+    a.e[0] = (T)p.extra_e[0];
+    a.e[1] = (T)p.extra_e[1];
+    const int grid = gate_grid<T>(s, a.ngroups, kUnroll);
+    switch (p.op) {
+    case P_SWAP: launch_pair_op<T, P_SWAP>(s, p.K, grid, a); break;
+    case P_Y: launch_pair_op<T, P_Y>(s, p.K, grid, a); break;
+    case P_H: launch_pair_op<T, P_H>(s, p.K, grid, a); break;
+    case P_RX: launch_pair_op<T, P_RX>(s, p.K, grid, a); break;
+    case P_RY: launch_pair_op<T, P_RY>(s, p.K, grid, a); break;
+    case P_MAT: launch_pair_op<T, P_MAT>(s, p.K, grid, a); break;
+    case P_DIAG: launch_pair_op<T, P_DIAG>(s, p.K, grid, a); break;
+    case P_PHASE_Y: launch_pair_op<T, P_PHASE_Y>(s, p.K, grid, a); break;
+    case P_ZERO: launch_pair_op<T, P_ZERO>(s, p.K, grid, a); break;
+    case P_GEN_SWAPI: launch_pair_op<T, P_GEN_SWAPI>(s, p.K, grid, a); break;
+    case P_ZERO_Y: launch_pair_op<T, P_ZERO_Y>(s, p.K, grid, a); break;
+    default: PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "internal: bad pair op");
+    }
+    PLK_CHECK_LAUNCH();
+    return PLK_OK;
+}
+
+template <class T> static int run_quad(plk_state s, const GatePlan &p, const WireGeom &g) {
+    QuadArgs<T> a;
+    a.mk = g.mk;
+    a.ngroups = s->length >> 2;
+    for (int i = 0; i < 4; i++) a.off[i] = g.local_off(i);
+    for (int j = 0; j < 32; j++) a.coef[j] = (T)p.coef[j];
+    const int grid = gate_grid<T>(s, a.ngroups, 1);
+    auto *sv = (c2_t<T> *)s->data;
+    switch (p.op) {
+    case Q_IXX: k_quad<T, Q_IXX><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case Q_IYY: k_quad<T, Q_IYY><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case Q_DIAG: k_quad<T, Q_DIAG><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case Q_MAT: k_quad<T, Q_MAT><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case Q_GEN_IXX: k_quad<T, Q_GEN_IXX><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case Q_GEN_IYY: k_quad<T, Q_GEN_IYY><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    default: PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "internal: bad quad op");
+    }
+    PLK_CHECK_LAUNCH();
+    return PLK_OK;
+}
+
+int run_plan(plk_state s, const GatePlan &p, const int64_t *wires) {
+    if (p.family == GatePlan::F_NOOP) return PLK_OK;
+    WireGeom g;
+    if (p.K > kMaxDenseWires && p.family != GatePlan::F_MRZ && p.family != GatePlan::F_GEN_MRZ)
+        PLK_FAIL(PLK_ERR_UNSUPPORTED, "too many wires");
+    if (p.family == GatePlan::F_MRZ || p.family == GatePlan::F_GEN_MRZ) {
+        uint64_t mask = 0;
+        for (int j = 0; j < p.K; j++) mask |= 1ULL << (s->nq - 1 - (int)wires[j]);
+        const int grid = s->dtype == PLK_C64 ? gate_grid<float>(s, s->length, 1) : gate_grid<double>(s, s->length, 1);
+        const bool gen = p.family == GatePlan::F_GEN_MRZ;
+        if (s->dtype == PLK_C64) {
+            if (gen) k_mrz<float, true><<<grid, kThreads, 0, s->stream>>>((float2 *)s->data, s->length, mask, 0, 0, 0, 0);
+            else k_mrz<float, false><<<grid, kThreads, 0, s->stream>>>((float2 *)s->data, s->length, mask,
+                                                                       (float)p.coef[0], (float)p.coef[1],
+                                                                       (float)p.coef[2], (float)p.coef[3]);
+        } else {
+            if (gen) k_mrz<double, true><<<grid, kThreads, 0, s->stream>>>((double2 *)s->data, s->length, mask, 0, 0, 0, 0);
+            else k_mrz<double, false><<<grid, kThreads, 0, s->stream>>>((double2 *)s->data, s->length, mask, p.coef[0],
+                                                                        p.coef[1], p.coef[2], p.coef[3]);
+        }
+        PLK_CHECK_LAUNCH();
+        return PLK_OK;
+    }
+    wire_geom(s->nq, wires, p.K, g);
+    if (p.family == GatePlan::F_PAIR)
+        return s->dtype == PLK_C64 ? run_pair<float>(s, p, g) : run_pair<double>(s, p, g);
+    if (p.family == GatePlan::F_QUAD)
+        return s->dtype == PLK_C64 ? run_quad<float>(s, p, g) : run_quad<double>(s, p, g);
+    PLK_FAIL(PLK_ERR_UNSUPPORTED, "internal: bad plan family");
+}
+
+// Dense matrix application (any k <= kMaxDenseWires).  `matrix` is complex128
+// row-major on the host; the adjoint is applied as the conjugate transpose.
+template <class T>
+static int run_dense(plk_state s, const double *matrix, const int64_t *wires, int K, bool adj) {
+    using V = c2_t<T>;
+    const int dim = 1 << K;
+    std::vector<V> hm((size_t)dim * dim);
+    for (int r = 0; r < dim; r++)
+        for (int c = 0; c < dim; c++) {
+            const size_t src = adj ? ((size_t)c * dim + r) : ((size_t)r * dim + c);
+            const double re = matrix[2 * src], im = adj ? -matrix[2 * src + 1] : matrix[2 * src + 1];
+            hm[(size_t)r * dim + c] = mk<V>((T)re, (T)im);
+        }
+    WireGeom g;
+    wire_geom(s->nq, wires, K, g);
+    std::vector<uint64_t> hoff(dim);
+    for (int i = 0; i < dim; i++) hoff[i] = g.local_off(i);
+    void *d_mat = nullptr, *d_off = nullptr;
+    PLK_CUDA(cudaMallocAsync(&d_mat, hm.size() * sizeof(V), s->stream));
+    PLK_CUDA(cudaMallocAsync(&d_off, hoff.size() * sizeof(uint64_t), s->stream));
+    PLK_CUDA(cudaMemcpyAsync(d_mat, hm.data(), hm.size() * sizeof(V), cudaMemcpyHostToDevice, s->stream));
+    PLK_CUDA(cudaMemcpyAsync(d_off, hoff.data(), hoff.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, s->stream));
+    const uint64_t ngroups = s->length >> K;
+    const int mat_smem = K <= kSmemMatWires ? 1 : 0;
+    const int gpb = dim >= kThreads ? 1 : kThreads / dim;
+    const size_t smem = (mat_smem ? (size_t)dim * dim * sizeof(V) : 0) + (size_t)gpb * dim * sizeof(V);
+    if (smem > 48 * 1024)
+        PLK_CUDA(cudaFuncSetAttribute(k_dense<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DeviceCtx *d = nullptr;
+    PLK_TRY(device_ctx(s->device, &d));
+    const uint64_t want = (ngroups + gpb - 1) / gpb;
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)d->sm_count * 8));
+    k_dense<T><<<grid, kThreads, smem, s->stream>>>((V *)s->data, (const V *)d_mat, (const uint64_t *)d_off, g.mk, K,
+                                                    ngroups, mat_smem);
+    PLK_CHECK_LAUNCH();
+    PLK_CUDA(cudaFreeAsync(d_mat, s->stream));
+    PLK_CUDA(cudaFreeAsync(d_off, s->stream));
+    // the host staging vectors are released on return: make the copies finish
+    PLK_CUDA(cudaStreamSynchronize(s->stream));
+    return PLK_OK;
+}
+
+int apply_matrix_impl(plk_state s, const double *matrix, const int64_t *wires, int nw, bool adj) {
+    if (!matrix) PLK_FAIL(PLK_ERR_INVALID_ARG, "null matrix");
+    if (nw < 1) PLK_FAIL(PLK_ERR_INVALID_ARG, "matrix needs at least one wire");
+    if (nw > kMaxDenseWires)
+        PLK_FAIL(PLK_ERR_UNSUPPORTED, "dense matrices on more than " + std::to_string(kMaxDenseWires) + " wires");
+    PLK_TRY(check_wires(s, wires, nw));
+    if (nw <= 2) {
+        GatePlan p;
+        std::memset(p.coef, 0, sizeof(p.coef));
+        const int dim = 1 << nw;
+        for (int r = 0; r < dim; r++)
+            for (int c = 0; c < dim; c++) {
+                const int src = adj ? (c * dim + r) : (r * dim + c);
+                p.coef[2 * (r * dim + c)] = matrix[2 * src];
+                p.coef[2 * (r * dim + c) + 1] = adj ? -matrix[2 * src + 1] : matrix[2 * src + 1];
+            }
+        if (nw == 1) set_pair(p, 1, P_MAT, 0, 1);
+        else {
+            p.family = GatePlan::F_QUAD;
+            p.K = 2;
+            p.op = Q_MAT;
+        }
+        return run_plan(s, p, wires);
+    }
+    return s->dtype == PLK_C64 ? run_dense<float>(s, matrix, wires, nw, adj)
+                               : run_dense<double>(s, matrix, wires, nw, adj);
+}
+
+int apply_gate_impl(plk_state s, int gate, const int64_t *wires, int nw, bool adj, const double *params, int np,
+                    const double *matrix) {
+    if (gate == PLK_GATE_MATRIX) return apply_matrix_impl(s, matrix, wires, nw, adj);
+    GatePlan p;
+    PLK_TRY(plan_gate(gate, nw, adj, params, np, p));
+    if (p.family == GatePlan::F_NOOP) return PLK_OK;
+    PLK_TRY(check_wires(s, wires, nw));
+    return run_plan(s, p, wires);
+}
+
+} // namespace plk
+
+using namespace plk;
+
+extern "C" {
+
+PLK_API int plk_gate_from_name(const char *name, int32_t *gate) {
+    if (!name || !gate) PLK_FAIL(PLK_ERR_INVALID_ARG, "null argument");
+    for (int i = 0; i < PLK_GATE_MATRIX; i++)
+        if (std::strcmp(kGates[i].name, name) == 0) {
+            *gate = i;
+            return PLK_OK;
+        }
+    *gate = -1;
+    PLK_FAIL(PLK_ERR_UNKNOWN_GATE, std::string("unknown gate name ") + name);
+}
+
+PLK_API int plk_gate_num_wires(int32_t gate) {
+    if (gate < 0 || gate >= PLK_GATE_COUNT) return 0;
+    return kGates[gate].nwires;
+}
+
+PLK_API int plk_gate_num_params(int32_t gate) {
+    if (gate < 0 || gate >= PLK_GATE_COUNT) return 0;
+    return kGates[gate].nparams;
+}
+
+PLK_API int plk_apply_gate(plk_state s, int32_t gate, const int64_t *wires, int32_t nw, int32_t adjoint,
+                           const double *params, int32_t np) {
+    PLK_TRY(check_state(s));
+    PLK_CUDA(cudaSetDevice(s->device));
+    if (gate == PLK_GATE_MATRIX) PLK_FAIL(PLK_ERR_INVALID_ARG, "use plk_apply_matrix for dense matrices");
+    return apply_gate_impl(s, gate, wires, nw, adjoint != 0, params, np, nullptr);
+}
+
+PLK_API int plk_apply_matrix(plk_state s, const double *matrix, const int64_t *wires, int32_t nw, int32_t adjoint) {
+    PLK_TRY(check_state(s));
+    PLK_CUDA(cudaSetDevice(s->device));
+    return apply_matrix_impl(s, matrix, wires, nw, adjoint != 0);
+}
+
+PLK_API int plk_apply_ops(plk_state s, const plk_op *ops, int32_t nops) {
+    PLK_TRY(check_state(s));
+    if (nops > 0 && !ops) PLK_FAIL(PLK_ERR_INVALID_ARG, "null ops");
+    PLK_CUDA(cudaSetDevice(s->device));
+    for (int i = 0; i < nops; i++) {
+        const plk_op &o = ops[i];
+        int st = apply_gate_impl(s, o.gate, o.wires, o.num_wires, o.adjoint != 0, o.params, o.num_params, o.matrix);
+        if (st != PLK_OK) {
+            set_error("op " + std::to_string(i) + ": " + last_error());
+            return st;
+        }
+    }
+    return PLK_OK;
+}
+
+PLK_API int plk_apply_generator(plk_state s, int32_t gate, const int64_t *wires, int32_t nw, int32_t adjoint,
+                                double *scale) {
+    (void)adjoint;
+    PLK_TRY(check_state(s));
+    PLK_CUDA(cudaSetDevice(s->device));
+    GatePlan p;
+    PLK_TRY(plan_generator(gate, nw, p));
+    PLK_TRY(check_wires(s, wires, nw));
+    PLK_TRY(run_plan(s, p, wires));
+    if (scale) *scale = p.scale;
+    return PLK_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,123 @@
+"""C ABI and module surface checks that need no GPU.
+
+* every function declared in include/plk_gb300.h is exported by
+  libplk_gb300.so (and nothing undeclared with the plk_ prefix);
+* the gate table agrees with the header's enum;
+* the pybind11 module exposes the reference module's classes and methods
+  (bindings/Bindings.cpp of the reference);
+* without a device, calls fail loudly (PLException / NO_DEVICE), never fall
+  back to a CPU path.
+"""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "plk_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"PLK_API\s+[\w\s\*]+?\b(plk_\w+)\s*\(", text)))
+
+
+def test_header_declares_functions():
+    fns = declared_functions()
+    assert len(fns) >= 40
+    assert "plk_adjoint_jacobian" in fns and "plk_apply_gate" in fns
+
+
+def test_library_exports_every_declared_symbol():
+    from pennylane_lightning_kokkos import _native as N
+
+    out = subprocess.run(["nm", "-D", "--defined-only", N.LIB_PATH], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (plk_\w+)", out))
+    declared = set(declared_functions())
+    assert declared <= exported, f"missing exports: {sorted(declared - exported)}"
+    assert exported <= declared, f"undeclared exports: {sorted(exported - declared)}"
+    for f in declared:
+        assert hasattr(N.lib, f)
+
+
+def test_gate_table_matches_header_enum():
+    from pennylane_lightning_kokkos import _native as N
+
+    text = open(HEADER).read()
+    enum = text[text.index("PLK_GATE_IDENTITY = 0"):text.index("PLK_GATE_COUNT")]
+    names = re.findall(r"PLK_GATE_(\w+)", enum)
+    assert len(names) == len(N.GATES)
+    for i, n in enumerate(N.GATES[:-1]):
+        g = C.c_int32(-1)
+        assert N.lib.plk_gate_from_name(n.encode(), C.byref(g)) == 0, n
+        assert g.value == i
+        assert names[i].replace("_", "") == n.upper().replace("_", "")
+    g = C.c_int32(0)
+    assert N.lib.plk_gate_from_name(b"NotAGate", C.byref(g)) == 2
+    assert "NotAGate" in N.last_error()
+    assert N.lib.plk_gate_num_wires(N.GATE_ID["Toffoli"]) == 3
+    assert N.lib.plk_gate_num_params(N.GATE_ID["Rot"]) == 3
+    assert N.lib.plk_gate_num_wires(N.GATE_ID["MultiRZ"]) == -1
+
+
+def test_module_surface_matches_reference():
+    import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
+
+    for bits in ("64", "128"):
+        for cls in ("LightningKokkos_C", "ObservableKokkos_C", "NamedObsKokkos_C", "HermitianObsKokkos_C",
+                    "TensorProdObsKokkos_C", "HamiltonianKokkos_C", "SparseHamiltonianKokkos_C",
+                    "OpsStructKokkos_C", "AdjointJacobianKokkos_C"):
+            assert hasattr(m, cls + bits), cls + bits
+        sv = getattr(m, "LightningKokkos_C" + bits)
+        for meth in ("Identity", "PauliX", "PauliY", "PauliZ", "Hadamard", "S", "T", "CNOT", "SWAP", "CSWAP",
+                     "Toffoli", "CY", "CZ", "PhaseShift", "ControlledPhaseShift", "RX", "RY", "RZ", "Rot", "CRX",
+                     "CRY", "CRZ", "CRot", "IsingXX", "IsingXY", "IsingYY", "IsingZZ", "MultiRZ",
+                     "SingleExcitation", "SingleExcitationMinus", "SingleExcitationPlus", "DoubleExcitation",
+                     "DoubleExcitationMinus", "DoubleExcitationPlus", "apply", "applyGenerator",
+                     "ExpectationValue", "probs", "GenerateSamples", "DeviceToHost", "HostToDevice",
+                     "setBasisState", "setStateVector", "numQubits", "dataLength", "resetKokkos"):
+            assert hasattr(sv, meth), meth
+        adj = getattr(m, "AdjointJacobianKokkos_C" + bits)
+        assert hasattr(adj, "create_ops_list") and hasattr(adj, "adjoint_jacobian")
+    for f in ("kokkos_start", "kokkos_end", "kokkos_config_info", "print_configuration", "InitializationSettings",
+              "PLException"):
+        assert hasattr(m, f)
+    s = m.InitializationSettings().set_device_id(0).set_num_threads(4)
+    assert s.get_device_id() == 0 and s.get_num_threads() == 4 and s.has_num_threads()
+
+
+def test_observables_build_without_device():
+    import numpy as np
+    import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
+
+    z0 = m.NamedObsKokkos_C128("PauliZ", [0])
+    x1 = m.NamedObsKokkos_C128("PauliX", [1])
+    t = m.TensorProdObsKokkos_C128([z0, x1])
+    h = m.HamiltonianKokkos_C128(np.array([0.5, -0.2]), [z0, t])
+    assert repr(z0) == "PauliZ[0]"
+    assert repr(t) == "PauliZ[0] @ PauliX[1]"
+    assert t.get_wires() == [0, 1]
+    assert h.get_wires() == [0, 1]
+    assert z0 == m.NamedObsKokkos_C128("PauliZ", [0]) and not (z0 == x1)
+    with pytest.raises(m.PLException):
+        m.TensorProdObsKokkos_C128([z0, m.NamedObsKokkos_C128("PauliX", [0])])  # overlapping wires
+    ops = m.AdjointJacobianKokkos_C128().create_ops_list(["RX", "CNOT"], [np.array([0.3]), np.array([])],
+                                                          [[0], [0, 1]], [False, False], [np.array([]), np.array([])])
+    assert "RX" in repr(ops)
+
+
+@pytest.mark.skipif(os.environ.get("CUDA_VISIBLE_DEVICES") is None and os.path.exists("/dev/nvidia0"),
+                    reason="a GPU is present")
+def test_no_device_fails_loudly():
+    import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
+    from pennylane_lightning_kokkos import _native as N
+
+    if N.device_count() > 0:
+        pytest.skip("a GPU is present")
+    with pytest.raises(m.PLException, match="no CUDA device"):
+        m.LightningKokkos_C128(3)
+    h = C.c_void_p()
+    assert N.lib.plk_state_create(3, 1, 0, C.byref(h)) == 6  # PLK_ERR_NO_DEVICE

@@ -5,6 +5,8 @@ Each test names the reference test it restates; the values live in
 """
 import math
 
+import zlib
+
 import numpy as np
 import pytest
 
@@ -178,7 +180,7 @@ def gate_matrix(name, nw, params, inverse=False):
 @pytest.mark.parametrize("name", sorted(ALL_GATES))
 def test_gates_unitary_and_inverse(name):
     nw, npar = ALL_GATES[name]
-    rng = np.random.default_rng(abs(hash(name)) % 2**32)
+    rng = np.random.default_rng(zlib.crc32(name.encode()))
     params = list(rng.uniform(0, 2 * np.pi, npar))
     m = gate_matrix(name, nw, params)
     np.testing.assert_allclose(m.conj().T @ m, np.eye(1 << nw), atol=1e-12)
