@@ -26,7 +26,8 @@ Printed JSON line:
                + CNOT ladder, 100-term Pauli Hamiltonian) in complex64 with
                FP64 accumulation vs complex128, seconds per gradient and the
                largest gradient difference
-`--impl reference` times the oracle instead.  For --gpus N
+`--impl reference` times the oracle (the CPU restatement of the reference
+functors) on the host cores instead.  For --gpus N
 under torchrun every rank runs an independent replica (weak scaling).
 """
 from __future__ import annotations
