@@ -221,6 +221,21 @@ PLK_API int plk_adjoint_jacobian(plk_state lambda, plk_state *hlambda, int32_t n
                                  const plk_op *ops, int32_t num_ops, const int64_t *trainable,
                                  int32_t num_trainable, double *jac);
 
+/* ---- allocation-free expectation values ------------------------------ */
+/* No counterpart in the reference.  For callers that may not allocate device
+ * memory — their device memory belongs to another allocator or to a fixed
+ * budget, where cudaMalloc/cudaFree would bypass it and synchronize the
+ * device: <PauliZ(wires[i])> (wires[i] = -1: the squared norm, i.e. Identity)
+ * of a caller-owned device state of 2^num_qubits amplitudes, written to the
+ * caller-owned device array `out` (count doubles) on `cuda_stream`, with no
+ * plk_state and no allocation.  Its scratch is a fixed library array
+ * (32.25 KiB per GPU, held until the process exits) shared by every call:
+ * count is limited to 16 (larger counts are rejected), and calls that overlap
+ * on the GPU race.  Runs on the current device; the first call on a device
+ * sets the scratch address up and should come before any stream capture. */
+PLK_API int plk_expval_pauliz_noalloc(const void *state, int32_t num_qubits, int32_t dtype, int32_t count,
+                                      const int64_t *wires, double *out, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
