@@ -1,0 +1,107 @@
+// df.cuh — FP64-class arithmetic on the FP32 pipe ("double-float").
+//
+// This GB300 executes 1.06 TFLOP/s of FP64 FMA against 71.6 TFLOP/s of FP32
+// FMA, so any FP64 instruction per amplitude caps a complex128 kernel at
+// 0.53 T FP64 instructions/s, well below HBM bandwidth.  These helpers carry
+// a value as an unevaluated sum hi + lo of two floats and use error-free
+// transformations on the FP32 pipe: the exact product a*b = p + e with
+// e = fma(a, b, -p) (Dekker/Kahan via FMA) and Knuth's two-sum for exact
+// addition.  Relative error per operation is about 2^-45 (lo terms below
+// 2^-48 are dropped), far inside the 1e-12 state tolerance of complex128.
+//
+// Conversions avoid the FP64 pipe: a double is split into hi (its top 24
+// significant bits, truncated) and lo (the next 23 bits) with integer
+// operations and one exact FP32 subtraction; a hi/lo pair becomes a double by
+// assembling each float's double encoding with integer operations and one
+// FP64 add.  Values below about 2^-97 in magnitude lose their lo part, values
+// below 2^-126 become zero; non-finite values are not supported on this path
+// (the native-FP64 kernels handle them).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace plk {
+
+struct DF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DF df_split(double x) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+    const unsigned hw = (unsigned)(u >> 32), lw = (unsigned)u;
+    const unsigned sign = hw & 0x80000000u;
+    const int e = (int)((hw >> 20) & 0x7ffu); // biased binary exponent of x
+    const int ef = e - 896;                    // same exponent, float bias
+    const unsigned m_top = ((hw & 0xfffffu) << 3) | (lw >> 29); // mantissa bits 51..29
+    const unsigned m_next = (lw >> 6) & 0x7fffffu;              // mantissa bits 28..6
+    DF r;
+    r.hi = (ef >= 1 && ef <= 254) ? __uint_as_float(sign | ((unsigned)ef << 23) | m_top) : 0.0f;
+    const int el = ef - 23; // float exponent of the unit in the last place of hi
+    if (el >= 1 && el <= 254) {
+        // (1 + m_next/2^23) 2^E - 2^E = m_next 2^(E-23): exact in FP32
+        const float F = __uint_as_float(((unsigned)el << 23) | m_next);
+        const float G = __uint_as_float((unsigned)el << 23);
+        r.lo = __uint_as_float(__float_as_uint(__fsub_rn(F, G)) | sign);
+    } else {
+        r.lo = 0.0f;
+    }
+    return r;
+}
+
+// The double with the same value as float f (normal floats; zero/denormal -> 0)
+__device__ __forceinline__ double df_f2d(float f) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned ef = (b >> 23) & 0xffu;
+    if (ef == 0) return 0.0;
+    const unsigned m = b & 0x7fffffu;
+    const unsigned hw = (b & 0x80000000u) | ((ef + 896u) << 20) | (m >> 3);
+    return __hiloint2double((int)hw, (int)(m << 29));
+}
+
+__device__ __forceinline__ double df_join(float hi, float lo) { return __dadd_rn(df_f2d(hi), df_f2d(lo)); }
+
+// (sh, sl) += a * b with a = ah + al, b = bh + bl; the accumulator is kept
+// unnormalised (sl collects the rounding errors).
+__device__ __forceinline__ void df_mac(float ah, float al, float bh, float bl, float &sh, float &sl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    const float s = __fadd_rn(sh, p);
+    const float bb = __fsub_rn(s, sh);
+    const float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(t, e));
+}
+
+// (sh, sl) += a with a = ah + al
+__device__ __forceinline__ void df_add(float ah, float al, float &sh, float &sl) {
+    const float s = __fadd_rn(sh, ah);
+    const float bb = __fsub_rn(s, sh);
+    const float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(ah, bb));
+    sh = s;
+    sl = __fadd_rn(sl, __fadd_rn(t, al));
+}
+
+__device__ __forceinline__ double df_result(float sh, float sl) {
+    const float s = __fadd_rn(sh, sl);
+    const float l = __fsub_rn(sl, __fsub_rn(s, sh));
+    return df_join(s, l);
+}
+
+// Host-side split of a coefficient (exact hi, rounded lo).
+inline void df_split_host(double x, float &hi, float &lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
+// Complex double-float amplitude
+struct CDF {
+    DF re, im;
+};
+
+__device__ __forceinline__ CDF cdf_split(double2 v) { return {df_split(v.x), df_split(v.y)}; }
+
+} // namespace plk

@@ -13,6 +13,7 @@
 // (simulator/GateFunctors.hpp); FMA contraction is allowed.
 #pragma once
 
+#include "df.cuh"
 #include "plk_internal.cuh"
 
 namespace plk {
@@ -29,6 +30,8 @@ enum PairOp : int {
     P_ZERO,       // x = y = 0
     P_GEN_SWAPI,  // x' = -i*sg*y, y' = i*sg*x                    coef: sg
     P_ZERO_Y,     // y = 0 (x untouched)                          (PhaseShift generator)
+    P_NEG_Y,      // y = -y (exact)                               (PauliZ, CZ, RZ/CRZ generators)
+    P_MULI_Y,     // y = i*sg*y (exact)                           coef: sg  (S, S^dag)
     P_NUM
 };
 
@@ -45,7 +48,13 @@ enum QuadOp : int {
 // Extra amplitudes of a pair group that are multiplied by a phase or zeroed.
 enum ExtraMode : int { X_NONE = 0, X_PHASE = 1, X_ZERO = 2 };
 
-template <int OP> __host__ __device__ constexpr bool pair_touches_x() { return OP != P_PHASE_Y && OP != P_ZERO_Y; }
+template <int OP> __host__ __device__ constexpr bool pair_touches_x() {
+    return OP != P_PHASE_Y && OP != P_ZERO_Y && OP != P_NEG_Y && OP != P_MULI_Y;
+}
+// Ops whose complex128 arithmetic can run on the FP32 pipe (see df.cuh).
+template <int OP> __host__ __device__ constexpr bool pair_has_df() {
+    return OP == P_H || OP == P_RX || OP == P_RY || OP == P_MAT || OP == P_DIAG || OP == P_PHASE_Y;
+}
 
 template <int OP, class V, class T>
 __device__ __forceinline__ void pair_op(V &x, V &y, const T *__restrict__ c) {
@@ -91,6 +100,10 @@ __device__ __forceinline__ void pair_op(V &x, V &y, const T *__restrict__ c) {
         y = mk<V>(0, 0);
     } else if constexpr (OP == P_ZERO_Y) {
         y = mk<V>(0, 0);
+    } else if constexpr (OP == P_NEG_Y) {
+        y = cneg(y);
+    } else if constexpr (OP == P_MULI_Y) {
+        y = c[0] > 0 ? mul_i(y) : mul_mi(y);
     } else if constexpr (OP == P_GEN_SWAPI) {
         const T sg = c[0];
         V t = x;
@@ -149,6 +162,121 @@ __device__ __forceinline__ void quad_op(V (&v)[4], const T *__restrict__ c) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// complex128 versions on the FP32 pipe.  Coefficients arrive split on the host
+// into hi (h) and lo (l) floats; every real output is a sum of at most eight
+// products accumulated as a double-float and rounded once to FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void df_first(float ah, float al, float bh, float bl, float &sh, float &sl) {
+    sh = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -sh);
+    e = __fmaf_rn(ah, bl, e);
+    sl = __fmaf_rn(al, bh, e);
+}
+
+// c0*a0 + c1*a1 (real coefficients c in (h, l), real operands a as DF)
+__device__ __forceinline__ double df_dot2(float c0h, float c0l, DF a0, float c1h, float c1l, DF a1) {
+    float sh, sl;
+    df_first(c0h, c0l, a0.hi, a0.lo, sh, sl);
+    df_mac(c1h, c1l, a1.hi, a1.lo, sh, sl);
+    return df_result(sh, sl);
+}
+
+// complex product e * v, e = (er, ei) in (h, l)
+__device__ __forceinline__ double2 df_cmul(const float *eh, const float *el, const CDF &v) {
+    double2 r;
+    r.x = df_dot2(eh[0], el[0], v.re, -eh[1], -el[1], v.im);
+    r.y = df_dot2(eh[0], el[0], v.im, eh[1], el[1], v.re);
+    return r;
+}
+
+// sum_j m_j v_j for complex m (interleaved in h/l) and complex v
+template <int N>
+__device__ __forceinline__ double2 df_cdot(const float *mh, const float *ml, const CDF *v) {
+    float rh, rl, ih, il;
+    df_first(mh[0], ml[0], v[0].re.hi, v[0].re.lo, rh, rl);
+    df_mac(-mh[1], -ml[1], v[0].im.hi, v[0].im.lo, rh, rl);
+    df_first(mh[0], ml[0], v[0].im.hi, v[0].im.lo, ih, il);
+    df_mac(mh[1], ml[1], v[0].re.hi, v[0].re.lo, ih, il);
+#pragma unroll
+    for (int j = 1; j < N; j++) {
+        df_mac(mh[2 * j], ml[2 * j], v[j].re.hi, v[j].re.lo, rh, rl);
+        df_mac(-mh[2 * j + 1], -ml[2 * j + 1], v[j].im.hi, v[j].im.lo, rh, rl);
+        df_mac(mh[2 * j], ml[2 * j], v[j].im.hi, v[j].im.lo, ih, il);
+        df_mac(mh[2 * j + 1], ml[2 * j + 1], v[j].re.hi, v[j].re.lo, ih, il);
+    }
+    return make_double2(df_result(rh, rl), df_result(ih, il));
+}
+
+template <int OP>
+__device__ __forceinline__ void pair_op_df(double2 &x, double2 &y, const float *__restrict__ h,
+                                           const float *__restrict__ l) {
+    if constexpr (OP == P_PHASE_Y) {
+        y = df_cmul(h, l, cdf_split(y));
+    } else if constexpr (OP == P_DIAG) {
+        x = df_cmul(h, l, cdf_split(x));
+        y = df_cmul(h + 2, l + 2, cdf_split(y));
+    } else {
+        const CDF a = cdf_split(x), b = cdf_split(y);
+        if constexpr (OP == P_H) {
+            // h[0] = 1/sqrt(2)
+            x = make_double2(df_dot2(h[0], l[0], a.re, h[0], l[0], b.re), df_dot2(h[0], l[0], a.im, h[0], l[0], b.im));
+            y = make_double2(df_dot2(h[0], l[0], a.re, -h[0], -l[0], b.re),
+                             df_dot2(h[0], l[0], a.im, -h[0], -l[0], b.im));
+        } else if constexpr (OP == P_RX) {
+            // x' = (c x.re - s y.im, c x.im + s y.re); y' = (c y.re - s x.im, c y.im + s x.re)
+            x = make_double2(df_dot2(h[0], l[0], a.re, -h[1], -l[1], b.im), df_dot2(h[0], l[0], a.im, h[1], l[1], b.re));
+            y = make_double2(df_dot2(h[0], l[0], b.re, -h[1], -l[1], a.im), df_dot2(h[0], l[0], b.im, h[1], l[1], a.re));
+        } else if constexpr (OP == P_RY) {
+            // x' = c x - s y; y' = s x + c y
+            x = make_double2(df_dot2(h[0], l[0], a.re, -h[1], -l[1], b.re),
+                             df_dot2(h[0], l[0], a.im, -h[1], -l[1], b.im));
+            y = make_double2(df_dot2(h[1], l[1], a.re, h[0], l[0], b.re), df_dot2(h[1], l[1], a.im, h[0], l[0], b.im));
+        } else if constexpr (OP == P_MAT) {
+            const CDF v[2] = {a, b};
+            x = df_cdot<2>(h, l, v);
+            y = df_cdot<2>(h + 4, l + 4, v);
+        }
+    }
+}
+
+template <int OP>
+__device__ __forceinline__ void quad_op_df(double2 (&v)[4], const float *__restrict__ h, const float *__restrict__ l) {
+    if constexpr (OP == Q_DIAG) {
+#pragma unroll
+        for (int i = 0; i < 4; i++) v[i] = df_cmul(h + 2 * i, l + 2 * i, cdf_split(v[i]));
+    } else {
+        CDF a[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) a[i] = cdf_split(v[i]);
+        if constexpr (OP == Q_MAT) {
+#pragma unroll
+            for (int r = 0; r < 4; r++) v[r] = df_cdot<4>(h + 8 * r, l + 8 * r, a);
+        } else if constexpr (OP == Q_IXX) {
+            // (cr v.re + sj w.im, cr v.im - sj w.re) with w the flipped partner
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const CDF &w = a[3 - i];
+                v[i] = make_double2(df_dot2(h[0], l[0], a[i].re, h[1], l[1], w.im),
+                                    df_dot2(h[0], l[0], a[i].im, -h[1], -l[1], w.re));
+            }
+        } else if constexpr (OP == Q_IYY) {
+            // 00, 11: (cr v.re - sj w.im, cr v.im + sj w.re); 01, 10: as IsingXX
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const CDF &w = a[3 - i];
+                const float sg = (i == 0 || i == 3) ? -1.0f : 1.0f;
+                v[i] = make_double2(df_dot2(h[0], l[0], a[i].re, sg * h[1], sg * l[1], w.im),
+                                    df_dot2(h[0], l[0], a[i].im, -sg * h[1], -sg * l[1], w.re));
+            }
+        }
+    }
+}
+
+template <int OP> __host__ __device__ constexpr bool quad_has_df() {
+    return OP == Q_IXX || OP == Q_IYY || OP == Q_DIAG || OP == Q_MAT;
+}
+
 // Host-side description of one gate (or generator) application.
 struct GatePlan {
     enum Family { F_NOOP = 0, F_PAIR, F_QUAD, F_MRZ, F_GEN_MRZ, F_DENSE };
@@ -174,6 +302,8 @@ template <class T> struct PairArgs {
     uint64_t off_extra[14];
     T coef[8];
     T e[2];
+    float ch[8], cl[8]; // coefficients split for the FP32-pipe complex128 path
+    float eh[2], el[2];
 };
 
 template <class T> struct QuadArgs {
@@ -181,6 +311,7 @@ template <class T> struct QuadArgs {
     uint64_t ngroups;
     uint64_t off[4];
     T coef[32];
+    float ch[32], cl[32];
 };
 
 } // namespace plk

@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "gate_ops.cuh"
@@ -105,9 +106,9 @@ int plan_gate(int gate, int nw, bool inv, const double *prm, int np, GatePlan &p
     case PLK_GATE_IDENTITY: p.family = GatePlan::F_NOOP; return PLK_OK;
     case PLK_GATE_PAULIX: set_pair(p, 1, P_SWAP, 0, 1); break;
     case PLK_GATE_PAULIY: set_pair(p, 1, P_Y, 0, 1); break;
-    case PLK_GATE_PAULIZ: set_pair(p, 1, P_PHASE_Y, 0, 1); p.coef[0] = -1; break;
-    case PLK_GATE_HADAMARD: set_pair(p, 1, P_H, 0, 1); break;
-    case PLK_GATE_S: set_pair(p, 1, P_PHASE_Y, 0, 1); p.coef[0] = 0; p.coef[1] = inv ? -1 : 1; break;
+    case PLK_GATE_PAULIZ: set_pair(p, 1, P_NEG_Y, 0, 1); break;
+    case PLK_GATE_HADAMARD: set_pair(p, 1, P_H, 0, 1); p.coef[0] = M_SQRT1_2; break;
+    case PLK_GATE_S: set_pair(p, 1, P_MULI_Y, 0, 1); p.coef[0] = inv ? -1 : 1; break;
     case PLK_GATE_T:
         set_pair(p, 1, P_PHASE_Y, 0, 1);
         p.coef[0] = std::cos(M_PI / 4);
@@ -137,7 +138,7 @@ int plan_gate(int gate, int nw, bool inv, const double *prm, int np, GatePlan &p
     // two-wire gates: local index bit 1 = wires[0] (control), bit 0 = wires[1]
     case PLK_GATE_CNOT: set_pair(p, 2, P_SWAP, 2, 3); break;
     case PLK_GATE_CY: set_pair(p, 2, P_Y, 2, 3); break;
-    case PLK_GATE_CZ: set_pair(p, 2, P_PHASE_Y, 2, 3); p.coef[0] = -1; break;
+    case PLK_GATE_CZ: set_pair(p, 2, P_NEG_Y, 2, 3); break;
     case PLK_GATE_SWAP: set_pair(p, 2, P_SWAP, 1, 2); break;
     case PLK_GATE_CONTROLLEDPHASESHIFT:
         set_pair(p, 2, P_PHASE_Y, 2, 3);
@@ -231,7 +232,7 @@ int plan_generator(int gate, int nw, GatePlan &p) {
     switch (gate) {
     case PLK_GATE_RX: set_pair(p, 1, P_SWAP, 0, 1); break;
     case PLK_GATE_RY: set_pair(p, 1, P_Y, 0, 1); break;
-    case PLK_GATE_RZ: set_pair(p, 1, P_PHASE_Y, 0, 1); p.coef[0] = -1; break;
+    case PLK_GATE_RZ: set_pair(p, 1, P_NEG_Y, 0, 1); break;
     case PLK_GATE_PHASESHIFT: set_pair(p, 1, P_ZERO_Y, 1, 0); p.scale = 1.0; break;
     case PLK_GATE_CONTROLLEDPHASESHIFT:
         set_pair(p, 2, P_ZERO, 0, 1);
@@ -241,8 +242,7 @@ int plan_generator(int gate, int nw, GatePlan &p) {
     case PLK_GATE_CRX: set_pair(p, 2, P_SWAP, 2, 3); set_extras_list(p, X_ZERO, {0, 1}); break;
     case PLK_GATE_CRY: set_pair(p, 2, P_Y, 2, 3); set_extras_list(p, X_ZERO, {0, 1}); break;
     case PLK_GATE_CRZ:
-        set_pair(p, 2, P_PHASE_Y, 2, 3);
-        p.coef[0] = -1;
+        set_pair(p, 2, P_NEG_Y, 2, 3);
         set_extras_list(p, X_ZERO, {0, 1});
         break;
     case PLK_GATE_ISINGXX: p.family = GatePlan::F_QUAD; p.K = 2; p.op = Q_GEN_IXX; break;
@@ -316,7 +316,7 @@ static void wire_geom(int nq, const int64_t *wires, int K, WireGeom &g) {
 // ---------------------------------------------------------------- kernels --
 constexpr int kUnroll = 2;
 
-template <class T, int OP, int K>
+template <class T, int OP, int K, bool DFP>
 __global__ void __launch_bounds__(kThreads) k_pair(c2_t<T> *__restrict__ sv, const PairArgs<T> a) {
     using V = c2_t<T>;
     constexpr bool TX = pair_touches_x<OP>();
@@ -337,20 +337,25 @@ __global__ void __launch_bounds__(kThreads) k_pair(c2_t<T> *__restrict__ sv, con
         for (int u = 0; u < kUnroll; u++) {
             const uint64_t g = g0 + (uint64_t)u * blockDim.x;
             if (g < a.ngroups) {
-                pair_op<OP>(x[u], y[u], a.coef);
+                if constexpr (DFP) pair_op_df<OP>(x[u], y[u], a.ch, a.cl);
+                else pair_op<OP>(x[u], y[u], a.coef);
                 if (TX) sv[base[u] + a.offA] = x[u];
                 sv[base[u] + a.offB] = y[u];
                 for (int j = 0; j < a.n_extra; j++) {
                     V *p = sv + base[u] + a.off_extra[j];
-                    if (a.extra_mode == X_PHASE) *p = cmul(*p, mk<V>(a.e[0], a.e[1]));
-                    else *p = mk<V>(0, 0);
+                    if (a.extra_mode == X_PHASE) {
+                        if constexpr (DFP) *p = df_cmul(a.eh, a.el, cdf_split(*p));
+                        else *p = cmul(*p, mk<V>(a.e[0], a.e[1]));
+                    } else {
+                        *p = mk<V>(0, 0);
+                    }
                 }
             }
         }
     }
 }
 
-template <class T, int OP>
+template <class T, int OP, bool DFP>
 __global__ void __launch_bounds__(kThreads) k_quad(c2_t<T> *__restrict__ sv, const QuadArgs<T> a) {
     using V = c2_t<T>;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
@@ -359,7 +364,8 @@ __global__ void __launch_bounds__(kThreads) k_quad(c2_t<T> *__restrict__ sv, con
         V v[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) v[i] = sv[base + a.off[i]];
-        quad_op<OP>(v, a.coef);
+        if constexpr (DFP) quad_op_df<OP>(v, a.ch, a.cl);
+        else quad_op<OP>(v, a.coef);
 #pragma unroll
         for (int i = 0; i < 4; i++) sv[base + a.off[i]] = v[i];
     }
@@ -446,15 +452,28 @@ template <class T> static int gate_grid(plk_state s, uint64_t work, int unroll) 
     return (int)std::max<uint64_t>(1, std::min(want, cap));
 }
 
-template <class T, int OP>
-static void launch_pair_op(plk_state s, int K, int grid, const PairArgs<T> &a) {
+template <class T, int OP, bool DFP>
+static void launch_pair_k(plk_state s, int K, int grid, const PairArgs<T> &a) {
     auto *sv = (c2_t<T> *)s->data;
     switch (K) {
-    case 1: k_pair<T, OP, 1><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
-    case 2: k_pair<T, OP, 2><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
-    case 3: k_pair<T, OP, 3><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
-    default: k_pair<T, OP, 4><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case 1: k_pair<T, OP, 1, DFP><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case 2: k_pair<T, OP, 2, DFP><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case 3: k_pair<T, OP, 3, DFP><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    default: k_pair<T, OP, 4, DFP><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
     }
+}
+
+// complex128 gates with arithmetic run on the FP32 pipe unless the native
+// FP64 path is requested (c128_use_df() == false)
+template <class T, int OP>
+static void launch_pair_op(plk_state s, int K, int grid, const PairArgs<T> &a) {
+    if constexpr (std::is_same_v<T, double> && pair_has_df<OP>()) {
+        if (c128_use_df()) {
+            launch_pair_k<T, OP, true>(s, K, grid, a);
+            return;
+        }
+    }
+    launch_pair_k<T, OP, false>(s, K, grid, a);
 }
 
 template <class T> static int run_pair(plk_state s, const GatePlan &p, const WireGeom &g) {
@@ -466,9 +485,14 @@ template <class T> static int run_pair(plk_state s, const GatePlan &p, const Wir
     a.n_extra = p.n_extra;
     a.extra_mode = p.extra_mode;
     for (int j = 0; j < p.n_extra; j++) a.off_extra[j] = g.local_off(p.extra_idx[j]);
-    for (int j = 0; j < 8; j++) a.coef[j] = (T)p.coef[j];
+    for (int j = 0; j < 8; j++) {
+        a.coef[j] = (T)p.coef[j];
+        df_split_host(p.coef[j], a.ch[j], a.cl[j]);
+    }
     a.e[0] = (T)p.extra_e[0];
     a.e[1] = (T)p.extra_e[1];
+    df_split_host(p.extra_e[0], a.eh[0], a.el[0]);
+    df_split_host(p.extra_e[1], a.eh[1], a.el[1]);
     const int grid = gate_grid<T>(s, a.ngroups, kUnroll);
     switch (p.op) {
     case P_SWAP: launch_pair_op<T, P_SWAP>(s, p.K, grid, a); break;
@@ -482,10 +506,23 @@ template <class T> static int run_pair(plk_state s, const GatePlan &p, const Wir
     case P_ZERO: launch_pair_op<T, P_ZERO>(s, p.K, grid, a); break;
     case P_GEN_SWAPI: launch_pair_op<T, P_GEN_SWAPI>(s, p.K, grid, a); break;
     case P_ZERO_Y: launch_pair_op<T, P_ZERO_Y>(s, p.K, grid, a); break;
+    case P_NEG_Y: launch_pair_op<T, P_NEG_Y>(s, p.K, grid, a); break;
+    case P_MULI_Y: launch_pair_op<T, P_MULI_Y>(s, p.K, grid, a); break;
     default: PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "internal: bad pair op");
     }
     PLK_CHECK_LAUNCH();
     return PLK_OK;
+}
+
+template <class T, int OP> static void launch_quad_op(plk_state s, int grid, const QuadArgs<T> &a) {
+    auto *sv = (c2_t<T> *)s->data;
+    if constexpr (std::is_same_v<T, double> && quad_has_df<OP>()) {
+        if (c128_use_df()) {
+            k_quad<T, OP, true><<<grid, kThreads, 0, s->stream>>>(sv, a);
+            return;
+        }
+    }
+    k_quad<T, OP, false><<<grid, kThreads, 0, s->stream>>>(sv, a);
 }
 
 template <class T> static int run_quad(plk_state s, const GatePlan &p, const WireGeom &g) {
@@ -493,16 +530,18 @@ template <class T> static int run_quad(plk_state s, const GatePlan &p, const Wir
     a.mk = g.mk;
     a.ngroups = s->length >> 2;
     for (int i = 0; i < 4; i++) a.off[i] = g.local_off(i);
-    for (int j = 0; j < 32; j++) a.coef[j] = (T)p.coef[j];
+    for (int j = 0; j < 32; j++) {
+        a.coef[j] = (T)p.coef[j];
+        df_split_host(p.coef[j], a.ch[j], a.cl[j]);
+    }
     const int grid = gate_grid<T>(s, a.ngroups, 1);
-    auto *sv = (c2_t<T> *)s->data;
     switch (p.op) {
-    case Q_IXX: k_quad<T, Q_IXX><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
-    case Q_IYY: k_quad<T, Q_IYY><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
-    case Q_DIAG: k_quad<T, Q_DIAG><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
-    case Q_MAT: k_quad<T, Q_MAT><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
-    case Q_GEN_IXX: k_quad<T, Q_GEN_IXX><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
-    case Q_GEN_IYY: k_quad<T, Q_GEN_IYY><<<grid, kThreads, 0, s->stream>>>(sv, a); break;
+    case Q_IXX: launch_quad_op<T, Q_IXX>(s, grid, a); break;
+    case Q_IYY: launch_quad_op<T, Q_IYY>(s, grid, a); break;
+    case Q_DIAG: launch_quad_op<T, Q_DIAG>(s, grid, a); break;
+    case Q_MAT: launch_quad_op<T, Q_MAT>(s, grid, a); break;
+    case Q_GEN_IXX: launch_quad_op<T, Q_GEN_IXX>(s, grid, a); break;
+    case Q_GEN_IYY: launch_quad_op<T, Q_GEN_IYY>(s, grid, a); break;
     default: PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "internal: bad quad op");
     }
     PLK_CHECK_LAUNCH();

@@ -106,6 +106,9 @@ int red_grid(const plk_state_s *s, uint64_t work_items);
 int elem_grid(plk_state s, uint64_t work_items);
 // Set the state to basis vector |index> (InitView / setBasisStateFunctor).
 int fill_basis(plk_state s, uint64_t index);
+// complex128 arithmetic on the FP32 pipe (default) or native FP64
+// (environment PLK_C128_ARITH=fp64).
+bool c128_use_df();
 
 // ----------------------------------------------------------------------------
 // complex arithmetic on float2 / double2

@@ -3,6 +3,7 @@
 // Replaces StateVectorKokkos's constructor / init / data movers
 // (simulator/StateVectorKokkos.hpp:140-574, 1596-1636) and the Kokkos
 // runtime configuration queries (util/GetConfigInfo.hpp).
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -45,6 +46,14 @@ int device_ctx(int device, DeviceCtx **out) {
     }
     *out = &g_dev[device];
     return PLK_OK;
+}
+
+bool c128_use_df() {
+    static const bool use = [] {
+        const char *v = std::getenv("PLK_C128_ARITH");
+        return !(v && std::string(v) == "fp64");
+    }();
+    return use;
 }
 
 int red_grid(const plk_state_s *s, uint64_t work_items) {
