@@ -221,6 +221,13 @@ PLK_API int plk_adjoint_jacobian(plk_state lambda, plk_state *hlambda, int32_t n
                                  const plk_op *ops, int32_t num_ops, const int64_t *trainable,
                                  int32_t num_trainable, double *jac);
 
+/* The same sweep without the work copy of lambda: `lambda` is overwritten (it
+ * ends as U_0^dag ... U_{n-1}^dag lambda).  Needs one state less, for callers
+ * that regenerate lambda instead of keeping it (checkpointed re-forward). */
+PLK_API int plk_adjoint_jacobian_inplace(plk_state lambda, plk_state *hlambda, int32_t num_obs,
+                                         const plk_op *ops, int32_t num_ops, const int64_t *trainable,
+                                         int32_t num_trainable, double *jac);
+
 /* ---- allocation-free expectation values ------------------------------ */
 /* No counterpart in the reference.  For callers that may not allocate device
  * memory — their device memory belongs to another allocator or to a fixed

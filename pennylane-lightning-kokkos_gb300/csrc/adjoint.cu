@@ -15,8 +15,10 @@
 // to 8 per launch; lambda is written by the last chunk only.
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
+#include "df.cuh"
 #include "gate_ops.cuh"
 #include "reduce.cuh"
 
@@ -85,6 +87,7 @@ template <class T> struct AdjArgs {
     uint64_t mrz_mask;
     T g[8];  // gate (U^dag) coefficients
     T e[2];  // phase on the other amplitudes (+/- excitation gates)
+    float gh[8], gl[8], eh[2], el[2]; // the same, split for the FP32-pipe complex128 path
 };
 
 // U^dag on the touched amplitudes (coefficients planned for adjoint = !inverse)
@@ -121,6 +124,37 @@ template <int KIND, class V, class T> __device__ __forceinline__ void adj_gate(V
 #pragma unroll
         for (int i = 0; i < 16; i++)
             if (i != 3 && i != 12) v[i] = cmul(v[i], mk<V>(a.e[0], a.e[1]));
+    }
+}
+
+// U^dag for complex128 on the FP32 pipe (double-float, see df.cuh)
+template <int KIND> __device__ __forceinline__ void adj_gate_df(double2 *v, const AdjArgs<double> &a) {
+    if constexpr (KIND == A_RX) pair_op_df<P_RX>(v[0], v[1], a.gh, a.gl);
+    else if constexpr (KIND == A_RY) pair_op_df<P_RY>(v[0], v[1], a.gh, a.gl);
+    else if constexpr (KIND == A_RZ) pair_op_df<P_DIAG>(v[0], v[1], a.gh, a.gl);
+    else if constexpr (KIND == A_PS) pair_op_df<P_PHASE_Y>(v[0], v[1], a.gh, a.gl);
+    else if constexpr (KIND == A_CRX) pair_op_df<P_RX>(v[2], v[3], a.gh, a.gl);
+    else if constexpr (KIND == A_CRY) pair_op_df<P_RY>(v[2], v[3], a.gh, a.gl);
+    else if constexpr (KIND == A_CRZ) pair_op_df<P_DIAG>(v[2], v[3], a.gh, a.gl);
+    else if constexpr (KIND == A_CPS) pair_op_df<P_PHASE_Y>(v[2], v[3], a.gh, a.gl);
+    else if constexpr (KIND == A_IXX || KIND == A_IYY || KIND == A_IZZ) {
+        double2 q[4] = {v[0], v[1], v[2], v[3]};
+        if constexpr (KIND == A_IXX) quad_op_df<Q_IXX>(q, a.gh, a.gl);
+        else if constexpr (KIND == A_IYY) quad_op_df<Q_IYY>(q, a.gh, a.gl);
+        else quad_op_df<Q_DIAG>(q, a.gh, a.gl);
+        for (int i = 0; i < 4; i++) v[i] = q[i];
+    } else if constexpr (KIND == A_IXY) pair_op_df<P_RX>(v[1], v[2], a.gh, a.gl);
+    else if constexpr (KIND == A_SE) pair_op_df<P_RY>(v[1], v[2], a.gh, a.gl);
+    else if constexpr (KIND == A_SEM || KIND == A_SEP) {
+        pair_op_df<P_RY>(v[1], v[2], a.gh, a.gl);
+        v[0] = df_cmul(a.eh, a.el, cdf_split(v[0]));
+        v[3] = df_cmul(a.eh, a.el, cdf_split(v[3]));
+    } else if constexpr (KIND == A_DE) pair_op_df<P_RY>(v[3], v[12], a.gh, a.gl);
+    else if constexpr (KIND == A_DEM || KIND == A_DEP) {
+        pair_op_df<P_RY>(v[3], v[12], a.gh, a.gl);
+#pragma unroll
+        for (int i = 0; i < 16; i++)
+            if (i != 3 && i != 12) v[i] = df_cmul(a.eh, a.el, cdf_split(v[i]));
     }
 }
 
@@ -173,7 +207,7 @@ template <int KIND, class V> __device__ __forceinline__ void adj_gen(V *v) {
 
 constexpr int kAdjObsPerLaunch = 8;
 
-template <class T, int KIND, int NV>
+template <class T, int KIND, int NV, bool DFP>
 __global__ void __launch_bounds__(kThreads)
     k_adj_fused(c2_t<T> *__restrict__ lam, c2_t<T> *const *__restrict__ hl, int nobs, int write_lambda,
                 const AdjArgs<T> a, double *partials, double *result, unsigned *counter, double post_scale) {
@@ -181,9 +215,7 @@ __global__ void __launch_bounds__(kThreads)
     constexpr int K = adj_K<KIND>();
     constexpr int D = 1 << K;
     constexpr uint32_t TOUCH = adj_touch<KIND>();
-    double acc[NV];
-#pragma unroll
-    for (int v = 0; v < NV; v++) acc[v] = 0.0;
+    DAcc dacc[NV]; // Im <H lambda_o | G lambda> per thread, on the FP32 pipe
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < a.ngroups; g += step) {
         uint64_t base;
@@ -197,14 +229,21 @@ __global__ void __launch_bounds__(kThreads)
             for (int i = 0; i < D; i++)
                 if (TOUCH & (1u << i)) lv[i] = lam[base + a.off[i]];
         }
-        // mu = G lambda (register copy)
-        V mu[D];
+        // mu = G lambda: the generators only move, negate, zero or multiply by
+        // +-i, so this copy is exact in either precision
+        CDF mu[D];
+        {
+            V m[D];
 #pragma unroll
-        for (int i = 0; i < D; i++) mu[i] = lv[i];
-        if constexpr (KIND == A_MRZ) {
-            if (__popcll(g & a.mrz_mask) & 1) mu[0] = cneg(mu[0]);
-        } else {
-            adj_gen<KIND>(mu);
+            for (int i = 0; i < D; i++) m[i] = lv[i];
+            if constexpr (KIND == A_MRZ) {
+                if (__popcll(g & a.mrz_mask) & 1) m[0] = cneg(m[0]);
+            } else {
+                adj_gen<KIND>(m);
+            }
+#pragma unroll
+            for (int i = 0; i < D; i++)
+                if (TOUCH & (1u << i)) mu[i] = to_cdf(m[i]);
         }
 #pragma unroll
         for (int o = 0; o < NV; o++) {
@@ -217,16 +256,20 @@ __global__ void __launch_bounds__(kThreads)
                     for (int i = 0; i < D; i++)
                         if (TOUCH & (1u << i)) hv[i] = hl[o][base + a.off[i]];
                 }
-                double im = 0.0;
 #pragma unroll
                 for (int i = 0; i < D; i++)
-                    if (TOUCH & (1u << i)) im += (double)hv[i].x * mu[i].y - (double)hv[i].y * mu[i].x;
-                acc[o] += im;
+                    if (TOUCH & (1u << i)) {
+                        const CDF h = to_cdf(hv[i]);
+                        dacc[o].mac(h.re, mu[i].im);
+                        dacc[o].msub(h.im, mu[i].re);
+                    }
                 if constexpr (KIND == A_MRZ) {
-                    const bool odd = __popcll(g & a.mrz_mask) & 1;
-                    hl[o][g] = odd ? cmul(hv[0], mk<V>(a.g[2], a.g[3])) : cmul(hv[0], mk<V>(a.g[0], a.g[1]));
+                    const int odd = __popcll(g & a.mrz_mask) & 1;
+                    if constexpr (DFP) hl[o][g] = df_cmul(a.gh + 2 * odd, a.gl + 2 * odd, cdf_split(hv[0]));
+                    else hl[o][g] = odd ? cmul(hv[0], mk<V>(a.g[2], a.g[3])) : cmul(hv[0], mk<V>(a.g[0], a.g[1]));
                 } else {
-                    adj_gate<KIND>(hv, a);
+                    if constexpr (DFP) adj_gate_df<KIND>(hv, a);
+                    else adj_gate<KIND>(hv, a);
 #pragma unroll
                     for (int i = 0; i < D; i++)
                         if (TOUCH & (1u << i)) hl[o][base + a.off[i]] = hv[i];
@@ -235,37 +278,53 @@ __global__ void __launch_bounds__(kThreads)
         }
         if (write_lambda) {
             if constexpr (KIND == A_MRZ) {
-                const bool odd = __popcll(g & a.mrz_mask) & 1;
-                lam[g] = odd ? cmul(lv[0], mk<V>(a.g[2], a.g[3])) : cmul(lv[0], mk<V>(a.g[0], a.g[1]));
+                const int odd = __popcll(g & a.mrz_mask) & 1;
+                if constexpr (DFP) lam[g] = df_cmul(a.gh + 2 * odd, a.gl + 2 * odd, cdf_split(lv[0]));
+                else lam[g] = odd ? cmul(lv[0], mk<V>(a.g[2], a.g[3])) : cmul(lv[0], mk<V>(a.g[0], a.g[1]));
             } else {
-                adj_gate<KIND>(lv, a);
+                if constexpr (DFP) adj_gate_df<KIND>(lv, a);
+                else adj_gate<KIND>(lv, a);
 #pragma unroll
                 for (int i = 0; i < D; i++)
                     if (TOUCH & (1u << i)) lam[base + a.off[i]] = lv[i];
             }
         }
     }
+    double acc[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) acc[v] = dacc[v].value();
     block_reduce_finish<NV>(acc, partials, result, counter, post_scale, nobs);
+}
+
+template <class T, int KIND, bool DFP>
+static void launch_fused_dfp(plk_state lam, int grid, c2_t<T> *const *d_hl, int nobs, int write_lambda,
+                             const AdjArgs<T> &a, double *result, double post_scale) {
+    auto &w = lam->ws;
+    auto *lp = (c2_t<T> *)lam->data;
+    if (nobs <= 1)
+        k_adj_fused<T, KIND, 1, DFP><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials,
+                                                                        result, w.d_counter, post_scale);
+    else if (nobs <= 2)
+        k_adj_fused<T, KIND, 2, DFP><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials,
+                                                                        result, w.d_counter, post_scale);
+    else if (nobs <= 4)
+        k_adj_fused<T, KIND, 4, DFP><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials,
+                                                                        result, w.d_counter, post_scale);
+    else
+        k_adj_fused<T, KIND, 8, DFP><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials,
+                                                                        result, w.d_counter, post_scale);
 }
 
 template <class T, int KIND>
 static int launch_fused_kind(plk_state lam, c2_t<T> *const *d_hl, int nobs, int write_lambda, const AdjArgs<T> &a,
                              double *result, double post_scale) {
     const int grid = red_grid(lam, a.ngroups);
-    auto &w = lam->ws;
-    auto *lp = (c2_t<T> *)lam->data;
-    if (nobs <= 1)
-        k_adj_fused<T, KIND, 1><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials, result,
-                                                                   w.d_counter, post_scale);
-    else if (nobs <= 2)
-        k_adj_fused<T, KIND, 2><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials, result,
-                                                                   w.d_counter, post_scale);
-    else if (nobs <= 4)
-        k_adj_fused<T, KIND, 4><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials, result,
-                                                                   w.d_counter, post_scale);
-    else
-        k_adj_fused<T, KIND, 8><<<grid, kThreads, 0, lam->stream>>>(lp, d_hl, nobs, write_lambda, a, w.d_partials, result,
-                                                                   w.d_counter, post_scale);
+    if constexpr (std::is_same_v<T, double>) {
+        if (c128_use_df()) launch_fused_dfp<T, KIND, true>(lam, grid, d_hl, nobs, write_lambda, a, result, post_scale);
+        else launch_fused_dfp<T, KIND, false>(lam, grid, d_hl, nobs, write_lambda, a, result, post_scale);
+    } else {
+        launch_fused_dfp<T, KIND, false>(lam, grid, d_hl, nobs, write_lambda, a, result, post_scale);
+    }
     PLK_CHECK_LAUNCH();
     return PLK_OK;
 }
@@ -294,9 +353,14 @@ static int fused_step(plk_state lam, c2_t<T> *const *d_hl, int nobs, const plk_o
     PLK_TRY(plan_gate(op.gate, op.num_wires, op.adjoint == 0, op.params, op.num_params, p)); // U^dag
     AdjArgs<T> a;
     std::memset(&a, 0, sizeof(a));
-    for (int j = 0; j < 8; j++) a.g[j] = (T)p.coef[j];
+    for (int j = 0; j < 8; j++) {
+        a.g[j] = (T)p.coef[j];
+        df_split_host(p.coef[j], a.gh[j], a.gl[j]);
+    }
     a.e[0] = (T)p.extra_e[0];
     a.e[1] = (T)p.extra_e[1];
+    df_split_host(p.extra_e[0], a.eh[0], a.el[0]);
+    df_split_host(p.extra_e[1], a.eh[1], a.el[1]);
     if (kind == A_MRZ) {
         a.ngroups = lam->length;
         for (int j = 0; j < op.num_wires; j++) a.mrz_mask |= 1ULL << (lam->nq - 1 - op.wires[j]);
@@ -392,8 +456,8 @@ using namespace plk;
 
 extern "C" {
 
-PLK_API int plk_adjoint_jacobian(plk_state lambda, plk_state *hlambda, int32_t nobs, const plk_op *ops, int32_t nops,
-                                 const int64_t *trainable, int32_t ntp, double *jac) {
+static int adjoint_checks(plk_state lambda, plk_state *hlambda, int32_t nobs, const plk_op *ops, int32_t nops,
+                          const int64_t *trainable, int32_t ntp, double *jac) {
     PLK_TRY(check_state(lambda));
     if (ntp <= 0) PLK_FAIL(PLK_ERR_INVALID_ARG, "No trainable parameters provided.");
     if (!trainable || !jac || (nops > 0 && !ops) || nobs < 0 || (nobs > 0 && !hlambda))
@@ -413,26 +477,50 @@ PLK_API int plk_adjoint_jacobian(plk_state lambda, plk_state *hlambda, int32_t n
         if (op.gate < 0 || op.gate >= PLK_GATE_COUNT) PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "unknown gate in op list");
         PLK_TRY(check_wires(lambda, op.wires, op.num_wires));
     }
+    return PLK_OK;
+}
+
+// Runs the sweep with `work` as lambda (overwritten) and the observable states
+// moved onto its stream for the duration of the call.
+static int adjoint_run(plk_state work, plk_state *hlambda, int32_t nobs, const plk_op *ops, int32_t nops,
+                       const int64_t *trainable, int32_t ntp, double *jac) {
+    std::vector<cudaStream_t> old_streams(nobs);
+    int st = PLK_OK;
+    for (int o = 0; o < nobs && st == PLK_OK; o++) {
+        old_streams[o] = hlambda[o]->stream;
+        st = plk_state_set_stream(hlambda[o], work->stream);
+    }
+    if (st == PLK_OK)
+        st = work->dtype == PLK_C64 ? adjoint_impl<float>(work, hlambda, nobs, ops, nops, trainable, ntp, jac)
+                                    : adjoint_impl<double>(work, hlambda, nobs, ops, nops, trainable, ntp, jac);
+    const std::string err = st == PLK_OK ? std::string() : last_error();
+    for (int o = 0; o < nobs; o++)
+        if (old_streams[o]) plk_state_set_stream(hlambda[o], old_streams[o]);
+    if (st != PLK_OK) set_error(err);
+    return st;
+}
+
+PLK_API int plk_adjoint_jacobian(plk_state lambda, plk_state *hlambda, int32_t nobs, const plk_op *ops, int32_t nops,
+                                 const int64_t *trainable, int32_t ntp, double *jac) {
+    PLK_TRY(adjoint_checks(lambda, hlambda, nobs, ops, nops, trainable, ntp, jac));
     PLK_CUDA(cudaSetDevice(lambda->device));
-    // work copy of lambda, on lambda's stream; observable states join that stream
+    // work copy of lambda, on lambda's stream
     plk_state work = nullptr;
     PLK_TRY(plk_state_create(lambda->nq, lambda->dtype, lambda->device, &work));
     int st = plk_state_set_stream(work, lambda->stream);
     if (st == PLK_OK) st = plk_state_copy(work, lambda);
-    std::vector<cudaStream_t> old_streams(nobs);
-    for (int o = 0; o < nobs && st == PLK_OK; o++) {
-        old_streams[o] = hlambda[o]->stream;
-        st = plk_state_set_stream(hlambda[o], lambda->stream);
-    }
-    if (st == PLK_OK)
-        st = lambda->dtype == PLK_C64 ? adjoint_impl<float>(work, hlambda, nobs, ops, nops, trainable, ntp, jac)
-                                      : adjoint_impl<double>(work, hlambda, nobs, ops, nops, trainable, ntp, jac);
+    if (st == PLK_OK) st = adjoint_run(work, hlambda, nobs, ops, nops, trainable, ntp, jac);
     const std::string err = st == PLK_OK ? std::string() : last_error();
-    for (int o = 0; o < nobs; o++)
-        if (old_streams[o]) plk_state_set_stream(hlambda[o], old_streams[o]);
     plk_state_destroy(work);
     if (st != PLK_OK) set_error(err);
     return st;
+}
+
+PLK_API int plk_adjoint_jacobian_inplace(plk_state lambda, plk_state *hlambda, int32_t nobs, const plk_op *ops,
+                                         int32_t nops, const int64_t *trainable, int32_t ntp, double *jac) {
+    PLK_TRY(adjoint_checks(lambda, hlambda, nobs, ops, nops, trainable, ntp, jac));
+    PLK_CUDA(cudaSetDevice(lambda->device));
+    return adjoint_run(lambda, hlambda, nobs, ops, nops, trainable, ntp, jac);
 }
 
 } // extern "C"

@@ -103,5 +103,38 @@ struct CDF {
 };
 
 __device__ __forceinline__ CDF cdf_split(double2 v) { return {df_split(v.x), df_split(v.y)}; }
+__device__ __forceinline__ CDF to_cdf(double2 v) { return cdf_split(v); }
+__device__ __forceinline__ CDF to_cdf(float2 v) { return {{v.x, 0.0f}, {v.y, 0.0f}}; }
+
+// (sh, sl) = a * b (first term of a sum)
+__device__ __forceinline__ void df_first(float ah, float al, float bh, float bl, float &sh, float &sl) {
+    sh = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -sh);
+    e = __fmaf_rn(ah, bl, e);
+    sl = __fmaf_rn(al, bh, e);
+}
+
+// Per-thread FP64-class accumulator on the FP32 pipe; converted to a double
+// once, at the end of the thread's loop, for the FP64 block reduction.
+struct DAcc {
+    float h = 0.0f, l = 0.0f;
+    __device__ __forceinline__ void mac(const DF &a, const DF &b) { df_mac(a.hi, a.lo, b.hi, b.lo, h, l); }
+    __device__ __forceinline__ void msub(const DF &a, const DF &b) { df_mac(-a.hi, -a.lo, b.hi, b.lo, h, l); }
+    __device__ __forceinline__ void add(const DF &a) { df_add(a.hi, a.lo, h, l); }
+    __device__ __forceinline__ void sub(const DF &a) { df_add(-a.hi, -a.lo, h, l); }
+    __device__ __forceinline__ double value() const { return df_result(h, l); }
+    __device__ __forceinline__ DF normalized() const {
+        const float s = __fadd_rn(h, l);
+        return {s, __fsub_rn(l, __fsub_rn(s, h))};
+    }
+};
+
+// |a|^2 as a double-float
+__device__ __forceinline__ DF df_norm2(const CDF &a) {
+    float h, l;
+    df_first(a.re.hi, a.re.lo, a.re.hi, a.re.lo, h, l);
+    df_mac(a.im.hi, a.im.lo, a.im.hi, a.im.lo, h, l);
+    return {h, l};
+}
 
 } // namespace plk

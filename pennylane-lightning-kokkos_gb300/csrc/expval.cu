@@ -9,6 +9,7 @@
 #include <map>
 #include <vector>
 
+#include "df.cuh"
 #include "gate_ops.cuh"
 #include "reduce.cuh"
 
@@ -34,16 +35,40 @@ template <class T, int OBS>
 __global__ void __launch_bounds__(kThreads)
     k_expval_pair(const c2_t<T> *__restrict__ sv, uint64_t ngroups, uint64_t mask_lo, uint64_t bit, double *partials,
                   double *result, unsigned *counter) {
-    double acc[1] = {0.0};
+    // per-thread sums on the FP32 pipe (double-float), FP64 across the block
+    DAcc a2; // X: Re(conj v0 v1); Y: Im(conj v0 v1); H: |v0|^2 - |v1|^2 + 2 Re(conj v0 v1)
+    constexpr int U = 2;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += step) {
-        const uint64_t i0 = ((g & ~mask_lo) << 1) | (g & mask_lo);
-        const c2_t<T> v0 = sv[i0], v1 = sv[i0 | bit];
-        const double ar = v0.x, ai = v0.y, br = v1.x, bi = v1.y;
-        if (OBS == OBS_X) acc[0] += 2.0 * (ar * br + ai * bi);
-        else if (OBS == OBS_Y) acc[0] += 2.0 * (ar * bi - ai * br);
-        else acc[0] += 0.70710678118654752440 * ((ar * ar + ai * ai) - (br * br + bi * bi) + 2.0 * (ar * br + ai * bi));
+    for (uint64_t g0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g0 < ngroups; g0 += step * U) {
+        c2_t<T> va[U], vb[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint64_t g = g0 + u * step;
+            const uint64_t i0 = ((g & ~mask_lo) << 1) | (g & mask_lo);
+            va[u] = g < ngroups ? sv[i0] : mk<c2_t<T>>(0, 0);
+            vb[u] = g < ngroups ? sv[i0 | bit] : mk<c2_t<T>>(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const CDF a = to_cdf(va[u]), b = to_cdf(vb[u]);
+            if (OBS == OBS_X) {
+                a2.mac(a.re, b.re);
+                a2.mac(a.im, b.im);
+            } else if (OBS == OBS_Y) {
+                a2.mac(a.re, b.im);
+                a2.msub(a.im, b.re);
+            } else {
+                a2.mac(a.re, a.re);
+                a2.mac(a.im, a.im);
+                a2.msub(b.re, b.re);
+                a2.msub(b.im, b.im);
+                const DF ar2 = {2.0f * a.re.hi, 2.0f * a.re.lo}, ai2 = {2.0f * a.im.hi, 2.0f * a.im.lo};
+                a2.mac(ar2, b.re);
+                a2.mac(ai2, b.im);
+            }
+        }
     }
+    double acc[1] = {OBS == OBS_H ? 0.70710678118654752440 * a2.value() : 2.0 * a2.value()};
     block_reduce_finish<1>(acc, partials, result, counter);
 }
 
@@ -56,16 +81,30 @@ __global__ void __launch_bounds__(kThreads)
     __shared__ uint64_t zm[NV];
     for (int v = threadIdx.x; v < NV; v += blockDim.x) zm[v] = v < nv ? zmask[v] : 0;
     __syncthreads();
+    DAcc dacc[NV];
+    constexpr int U = 4; // amplitudes in flight per thread
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += step * U) {
+        c2_t<T> v[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint64_t k = k0 + u * step;
+            v[u] = k < n ? sv[k] : mk<c2_t<T>>(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint64_t k = k0 + u * step;
+            const DF p = df_norm2(to_cdf(v[u]));
+#pragma unroll
+            for (int w = 0; w < NV; w++) {
+                if (__popcll(k & zm[w]) & 1) dacc[w].sub(p);
+                else dacc[w].add(p);
+            }
+        }
+    }
     double acc[NV];
 #pragma unroll
-    for (int v = 0; v < NV; v++) acc[v] = 0.0;
-    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
-        const c2_t<T> a = sv[k];
-        const double p = (double)a.x * a.x + (double)a.y * a.y;
-#pragma unroll
-        for (int v = 0; v < NV; v++) acc[v] += (__popcll(k & zm[v]) & 1) ? -p : p;
-    }
+    for (int v = 0; v < NV; v++) acc[v] = dacc[v].value();
     block_reduce_finish<NV>(acc, partials, result, counter, 1.0, nv);
 }
 
@@ -111,13 +150,27 @@ template <class T>
 __global__ void __launch_bounds__(kThreads)
     k_inner(const c2_t<T> *__restrict__ x, const c2_t<T> *__restrict__ y, uint64_t n, double *partials, double *result,
             unsigned *counter) {
-    double acc[2] = {0.0, 0.0};
+    DAcc re, im;
+    constexpr int U = 2;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
-        const c2_t<T> a = x[k], b = y[k];
-        acc[0] += (double)a.x * b.x + (double)a.y * b.y;
-        acc[1] += (double)a.x * b.y - (double)a.y * b.x;
+    for (uint64_t k0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += step * U) {
+        c2_t<T> xa[U], ya[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint64_t k = k0 + u * step;
+            xa[u] = k < n ? x[k] : mk<c2_t<T>>(0, 0);
+            ya[u] = k < n ? y[k] : mk<c2_t<T>>(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const CDF a = to_cdf(xa[u]), b = to_cdf(ya[u]);
+            re.mac(a.re, b.re);
+            re.mac(a.im, b.im);
+            im.mac(a.re, b.im);
+            im.msub(a.im, b.re);
+        }
     }
+    double acc[2] = {re.value(), im.value()};
     block_reduce_finish<2>(acc, partials, result, counter);
 }
 
@@ -167,7 +220,8 @@ __global__ void __launch_bounds__(kThreads)
 // share x form one group; a group costs one pass over the state.
 struct PauliTerm {
     uint64_t z;
-    double cr, ci; // c_j * i^ny
+    double cr, ci;           // c_j * i^ny
+    float crh, crl, cih, cil; // the same, split for the FP32-pipe accumulation
 };
 
 struct PauliGroup {
@@ -204,7 +258,10 @@ static int build_pauli_groups(plk_state s, int nterms, const double *coeffs, con
             cr = nr;
             ci = ni;
         }
-        by_x[x].push_back({z, cr, ci});
+        PauliTerm pt{z, cr, ci, 0, 0, 0, 0};
+        df_split_host(cr, pt.crh, pt.crl);
+        df_split_host(ci, pt.cih, pt.cil);
+        by_x[x].push_back(pt);
     }
     groups.clear();
     terms.clear();
@@ -227,39 +284,51 @@ __global__ void __launch_bounds__(kThreads)
     extern __shared__ PauliTerm sterm[];
     for (int i = threadIdx.x; i < nt; i += blockDim.x) sterm[i] = terms[i];
     __syncthreads();
-    double acc[1] = {0.0};
+    // coefficients of the group as double-floats (split once per thread)
+    DAcc total;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     if (x == 0) {
         for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
-            const c2_t<T> a = sv[k];
-            const double p = (double)a.x * a.x + (double)a.y * a.y;
-            double f = 0.0;
-            for (int t = 0; t < nt; t++) f += (__popcll(k & sterm[t].z) & 1) ? -sterm[t].cr : sterm[t].cr;
-            acc[0] += p * f;
+            const DF p = df_norm2(to_cdf(sv[k]));
+            DAcc f;
+            for (int t = 0; t < nt; t++) {
+                const DF c = {sterm[t].crh, sterm[t].crl};
+                if (__popcll(k & sterm[t].z) & 1) f.sub(c);
+                else f.add(c);
+            }
+            total.mac(p, f.normalized());
         }
     } else {
         const uint64_t half = n >> 1;
         for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < half; g += step) {
             const uint64_t m = ((g & ~pmask_lo) << 1) | (g & pmask_lo);
             const uint64_t mp = m ^ x;
-            const c2_t<T> a = sv[m], b = sv[mp];
-            double fr_mp = 0, fi_mp = 0, fr_m = 0, fi_m = 0;
+            const CDF a = to_cdf(sv[m]), b = to_cdf(sv[mp]);
+            // F1 = Re f(m') + Re f(m), F2 = Im f(m) - Im f(m')
+            DAcc f1, f2;
             for (int t = 0; t < nt; t++) {
                 const PauliTerm tt = sterm[t];
-                const double s1 = (__popcll(mp & tt.z) & 1) ? -1.0 : 1.0;
-                const double s0 = (__popcll(m & tt.z) & 1) ? -1.0 : 1.0;
-                fr_mp += s1 * tt.cr;
-                fi_mp += s1 * tt.ci;
-                fr_m += s0 * tt.cr;
-                fi_m += s0 * tt.ci;
+                const bool s1 = __popcll(mp & tt.z) & 1, s0 = __popcll(m & tt.z) & 1;
+                if (s1 == s0) {
+                    const DF c = {2.0f * tt.crh, 2.0f * tt.crl};
+                    if (s0) f1.sub(c);
+                    else f1.add(c);
+                } else {
+                    const DF c = {2.0f * tt.cih, 2.0f * tt.cil};
+                    if (s0) f2.sub(c); // s0 set: -ci from f(m), s1 clear: +ci from -f(m')
+                    else f2.add(c);
+                }
             }
-            // Re[conj(a) b f(mp)] + Re[conj(b) a f(m)]
-            const double abr = (double)a.x * b.x + (double)a.y * b.y; // Re conj(a) b
-            const double abi = (double)a.x * b.y - (double)a.y * b.x; // Im conj(a) b
-            acc[0] += abr * fr_mp - abi * fi_mp;
-            acc[0] += abr * fr_m + abi * fi_m; // conj(b) a = conj(conj(a) b)
+            DAcc ab_re, ab_im; // conj(a) b
+            ab_re.mac(a.re, b.re);
+            ab_re.mac(a.im, b.im);
+            ab_im.mac(a.re, b.im);
+            ab_im.msub(a.im, b.re);
+            total.mac(ab_re.normalized(), f1.normalized());
+            total.mac(ab_im.normalized(), f2.normalized());
         }
     }
+    double acc[1] = {total.value()};
     block_reduce_finish<1>(acc, partials, result, counter);
 }
 

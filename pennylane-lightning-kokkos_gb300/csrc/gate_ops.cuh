@@ -167,13 +167,6 @@ __device__ __forceinline__ void quad_op(V (&v)[4], const T *__restrict__ c) {
 // into hi (h) and lo (l) floats; every real output is a sum of at most eight
 // products accumulated as a double-float and rounded once to FP64.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void df_first(float ah, float al, float bh, float bl, float &sh, float &sl) {
-    sh = __fmul_rn(ah, bh);
-    float e = __fmaf_rn(ah, bh, -sh);
-    e = __fmaf_rn(ah, bl, e);
-    sl = __fmaf_rn(al, bh, e);
-}
-
 // c0*a0 + c1*a1 (real coefficients c in (h, l), real operands a as DF)
 __device__ __forceinline__ double df_dot2(float c0h, float c0l, DF a0, float c1h, float c1l, DF a1) {
     float sh, sl;

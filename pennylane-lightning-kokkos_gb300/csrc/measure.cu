@@ -19,6 +19,7 @@
 #include <cstring>
 #include <vector>
 
+#include "df.cuh"
 #include "plk_internal.cuh"
 
 namespace plk {
@@ -27,8 +28,8 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) k_probs(const c2_t<T> *__restrict__ sv, double *__restrict__ p, uint64_t n) {
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
-        const c2_t<T> a = sv[k];
-        p[k] = (double)a.x * a.x + (double)a.y * a.y;
+        const DF q = df_norm2(to_cdf(sv[k])); // |psi_k|^2 on the FP32 pipe, one FP64 add
+        p[k] = df_result(q.hi, q.lo);
     }
 }
 

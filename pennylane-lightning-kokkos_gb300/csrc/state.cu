@@ -60,7 +60,7 @@ int red_grid(const plk_state_s *s, uint64_t work_items) {
     DeviceCtx *d = nullptr;
     if (device_ctx(s->device, &d) != PLK_OK) return 1;
     uint64_t want = (work_items + kThreads - 1) / kThreads;
-    uint64_t cap = (uint64_t)d->sm_count * 4;
+    uint64_t cap = (uint64_t)d->sm_count * 6;
     if (cap > (uint64_t)kMaxRedBlocks) cap = kMaxRedBlocks;
     if (want > cap) want = cap;
     return want < 1 ? 1 : (int)want;

@@ -96,6 +96,8 @@ _SIGS = {
     "plk_generate_samples": ([_vp, C.c_uint64, C.c_uint64, _i64p], C.c_int),
     "plk_adjoint_jacobian": ([_vp, C.POINTER(_vp), C.c_int32, C.POINTER(PlkOp), C.c_int32, _i64p, C.c_int32, _dp],
                              C.c_int),
+    "plk_adjoint_jacobian_inplace": ([_vp, C.POINTER(_vp), C.c_int32, C.POINTER(PlkOp), C.c_int32, _i64p, C.c_int32,
+                                      _dp], C.c_int),
     "plk_expval_pauliz_noalloc": ([_vp, C.c_int32, C.c_int32, C.c_int32, _i64p, _dp, _vp], C.c_int),
 }
 for _name, (_args, _res) in _SIGS.items():
