@@ -243,6 +243,64 @@ PLK_API int plk_adjoint_jacobian_inplace(plk_state lambda, plk_state *hlambda, i
 PLK_API int plk_expval_pauliz_noalloc(const void *state, int32_t num_qubits, int32_t dtype, int32_t count,
                                       const int64_t *wires, double *out, void *cuda_stream);
 
+/* ---- gate matrices ---------------------------------------------------- */
+/* Dense matrix (row-major complex128 pairs, 4^num_wires of them; wires[0] is
+ * the most significant bit of the row index) of a named gate, built from the
+ * same gate plans as the state kernels.  The reference builds these on the
+ * Python side (pennylane.operation.Operation.matrix, consumed by
+ * StateVectorKokkos::applyMultiQubitOp, StateVectorKokkos.hpp:763-796). */
+PLK_API int plk_gate_matrix(int32_t gate, const double *params, int32_t num_params, int32_t adjoint,
+                            int32_t num_wires, double *out);
+
+/* ---- batched circuits ------------------------------------------------- */
+/* Many independent circuits (own qubit count 4..30, own gates and
+ * parameters, own Pauli-sum observable) evaluated together: for every circuit
+ * the forward pass from |0...0>, <H> and the adjoint gradient d<H>/dtheta of
+ * its trainable parameters, in one persistent launch (replayed as a CUDA
+ * graph).  Per circuit this is what the reference's device does one tape at
+ * a time: apply the tape (StateVectorKokkos::applyOperation,
+ * StateVectorKokkos.hpp:585-676), the Hamiltonian expectation
+ * (ObservablesKokkos.hpp:484-494) and AdjointJacobianKokkos::adjointJacobian
+ * (AdjointDiffKokkos.hpp:404-478).  Gates act on at most 4 wires (MultiRZ on
+ * any number); Rot and CRot are decomposed into RZ RY RZ (CRZ CRY CRZ) and
+ * each of their three parameters is differentiable.  Parameters of a circuit
+ * form a flat list in op order; `trainable` lists sorted indices into it
+ * (NULL: all).  The observable is packed as in plk_expval_pauli_sum. */
+typedef struct plk_batch_s *plk_batch;
+PLK_API int plk_batch_create(int32_t dtype, int32_t device, plk_batch *out);
+PLK_API int plk_batch_destroy(plk_batch b);
+PLK_API int plk_batch_add(plk_batch b, int32_t num_qubits, const plk_op *ops, int32_t num_ops,
+                          const int64_t *trainable, int32_t num_trainable, int32_t num_terms,
+                          const double *coeffs, const int64_t *offsets, const int64_t *wires,
+                          const char *letters, int64_t *index);
+/* totals: circuits, flat parameters, Jacobian entries (sum of trainables) */
+PLK_API int plk_batch_info(plk_batch b, int64_t *num_circuits, int64_t *num_params, int64_t *num_jac);
+PLK_API int plk_batch_circuit_info(plk_batch b, int64_t circuit, int64_t *param_offset, int32_t *num_params,
+                                   int64_t *jac_offset, int32_t *num_trainable);
+/* replaces all parameters (flat, circuits in the order they were added) */
+PLK_API int plk_batch_set_params(plk_batch b, const double *params, int64_t count);
+/* expvals: one per circuit; jac: flat, circuit c at its jac_offset, in the
+ * order of its trainable list.  Either may be NULL.  Synchronous. */
+PLK_API int plk_batch_run(plk_batch b, double *expvals, double *jac);
+/* Device variant for callers that keep parameters and results on the GPU:
+ * enqueues the run on cuda_stream (NULL: the batch's stream) without host
+ * synchronisation or allocation after the first call of a configuration. */
+PLK_API int plk_batch_run_device(plk_batch b, const double *d_params, double *d_expvals, double *d_jac,
+                                 void *cuda_stream);
+/* device time (CUDA events) and kernel launches of the last plk_batch_run */
+PLK_API int plk_batch_last_time(plk_batch b, double *ms, int64_t *launches);
+/* launch configuration: CTAs per cluster (1, 2, 4, 8), threads per CTA (256,
+ * 512), circuits of at most smem_qubits qubits run in shared memory, circuits
+ * of at least cluster_min_qubits qubits are shared by a cluster */
+PLK_API int plk_batch_set_config(plk_batch b, int32_t cluster, int32_t threads, int32_t smem_qubits,
+                                 int32_t cluster_min_qubits);
+PLK_API int plk_batch_get_config(plk_batch b, int32_t *cluster, int32_t *threads, int32_t *smem_qubits,
+                                 int32_t *cluster_min_qubits);
+PLK_API int plk_batch_set_graph(plk_batch b, int32_t use_graph);
+/* autotuner: times a grid of configurations on this batch (median of reps
+ * runs each) and keeps the fastest; a text report goes to `report` */
+PLK_API int plk_batch_tune(plk_batch b, int32_t reps, char *report, int32_t report_len);
+
 #ifdef __cplusplus
 }
 #endif

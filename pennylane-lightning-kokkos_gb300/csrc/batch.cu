@@ -1,0 +1,1573 @@
+// batch.cu — batched circuits: forward pass, <H> and adjoint gradient of many
+// independent circuits in one persistent launch (device side in
+// batch_engine.cuh).
+//
+// The per-circuit work restates, for every circuit of the batch,
+//   StateVectorKokkos::applyOperation over the tape (StateVectorKokkos.hpp:
+//     585-676), the Hamiltonian expectation (ObservablesKokkos.hpp:484-494,
+//     MeasuresKokkos.hpp:354-366) and
+//   AdjointJacobianKokkos::adjointJacobian (AdjointDiffKokkos.hpp:404-478):
+//     walking the ops backwards, jac[t] = -2 * scale * Im <H lambda | G lambda>
+//     before lambda <- U^dag lambda and H lambda <- U^dag H lambda.
+// The reference runs this one circuit at a time (the Python device loops over
+// tapes); here a batch is compiled once into register windows and a CUDA
+// graph replays [parameters H2D, matrix preparation, engine, results D2H].
+//
+// Gate matrices come from the same gate plans as the per-state kernels
+// (plan_gate / plan_generator), expanded to dense matrices on the host.  A
+// parametric gate's entries are trigonometric polynomials of degree one in
+// theta/2, U(theta) = A0 + cos(theta/2) A1 + sin(theta/2) A2 + cos(theta) A3
+// + sin(theta) A4; the five coefficient matrices are fitted once per gate
+// from five angles (checked at two more), so the device rebuilds U from the
+// parameter vector without gate-specific code.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "batch_engine.cuh"
+#include "gate_ops.cuh"
+
+namespace plk {
+
+int plan_gate(int gate, int nw, bool inv, const double *prm, int np, GatePlan &p);
+int plan_generator(int gate, int nw, GatePlan &p);
+
+// ------------------------------------------------------- dense gate plans --
+// Applies a plan to the local amplitudes v[0 .. 2^K) (bit K-1-j <-> wires[j]).
+static void apply_plan_host(const GatePlan &p, int K, double2 *v) {
+    const int D = 1 << K;
+    switch (p.family) {
+    case GatePlan::F_NOOP: return;
+    case GatePlan::F_PAIR: {
+        double2 &x = v[p.a], &y = v[p.b];
+        switch (p.op) {
+        case P_SWAP: pair_op<P_SWAP>(x, y, p.coef); break;
+        case P_Y: pair_op<P_Y>(x, y, p.coef); break;
+        case P_H: pair_op<P_H>(x, y, p.coef); break;
+        case P_RX: pair_op<P_RX>(x, y, p.coef); break;
+        case P_RY: pair_op<P_RY>(x, y, p.coef); break;
+        case P_MAT: pair_op<P_MAT>(x, y, p.coef); break;
+        case P_DIAG: pair_op<P_DIAG>(x, y, p.coef); break;
+        case P_PHASE_Y: pair_op<P_PHASE_Y>(x, y, p.coef); break;
+        case P_ZERO: pair_op<P_ZERO>(x, y, p.coef); break;
+        case P_GEN_SWAPI: pair_op<P_GEN_SWAPI>(x, y, p.coef); break;
+        case P_ZERO_Y: pair_op<P_ZERO_Y>(x, y, p.coef); break;
+        case P_NEG_Y: pair_op<P_NEG_Y>(x, y, p.coef); break;
+        case P_MULI_Y: pair_op<P_MULI_Y>(x, y, p.coef); break;
+        default: break;
+        }
+        for (int i = 0; i < p.n_extra; i++) {
+            double2 &e = v[p.extra_idx[i]];
+            if (p.extra_mode == X_PHASE) e = cmul(e, mk<double2>(p.extra_e[0], p.extra_e[1]));
+            else if (p.extra_mode == X_ZERO) e = mk<double2>(0, 0);
+        }
+        return;
+    }
+    case GatePlan::F_QUAD: {
+        double2 q[4] = {v[0], v[1], v[2], v[3]};
+        switch (p.op) {
+        case Q_IXX: quad_op<Q_IXX>(q, p.coef); break;
+        case Q_IYY: quad_op<Q_IYY>(q, p.coef); break;
+        case Q_DIAG: quad_op<Q_DIAG>(q, p.coef); break;
+        case Q_MAT: quad_op<Q_MAT>(q, p.coef); break;
+        case Q_GEN_IXX: quad_op<Q_GEN_IXX>(q, p.coef); break;
+        case Q_GEN_IYY: quad_op<Q_GEN_IYY>(q, p.coef); break;
+        default: break;
+        }
+        for (int i = 0; i < 4; i++) v[i] = q[i];
+        return;
+    }
+    case GatePlan::F_MRZ:
+        for (int i = 0; i < D; i++) {
+            const bool odd = __builtin_popcount((unsigned)i) & 1;
+            v[i] = cmul(v[i], odd ? mk<double2>(p.coef[2], p.coef[3]) : mk<double2>(p.coef[0], p.coef[1]));
+        }
+        return;
+    case GatePlan::F_GEN_MRZ:
+        for (int i = 0; i < D; i++)
+            if (__builtin_popcount((unsigned)i) & 1) v[i] = cneg(v[i]);
+        return;
+    default: return;
+    }
+}
+
+static void plan_dense(const GatePlan &p, int K, std::vector<double2> &M) {
+    const int D = 1 << K;
+    M.assign((size_t)D * D, mk<double2>(0, 0));
+    std::vector<double2> v(D);
+    for (int c = 0; c < D; c++) {
+        std::fill(v.begin(), v.end(), mk<double2>(0, 0));
+        v[c] = mk<double2>(1, 0);
+        apply_plan_host(p, K, v.data());
+        for (int r = 0; r < D; r++) M[(size_t)r * D + c] = v[r];
+    }
+}
+
+static int gate_dense(int gate, int K, bool inv, double theta, std::vector<double2> &M) {
+    GatePlan p;
+    const double prm[3] = {theta, 0.0, 0.0};
+    PLK_TRY(plan_gate(gate, K, inv, prm, 3, p));
+    plan_dense(p, p.family == GatePlan::F_NOOP ? K : (p.K > 0 ? p.K : K), M);
+    return PLK_OK;
+}
+
+static void trig5(double th, double *f) {
+    f[0] = 1.0;
+    f[1] = std::cos(th / 2);
+    f[2] = std::sin(th / 2);
+    f[3] = std::cos(th);
+    f[4] = std::sin(th);
+}
+
+// Coefficient matrices A0..A4 of U(theta) (D*D complex each).
+static int fit_gate(int gate, int K, bool inv, int nparams, std::vector<double2> &A) {
+    const int D = 1 << K;
+    const size_t DD = (size_t)D * D;
+    A.assign(5 * DD, mk<double2>(0, 0));
+    std::vector<double2> U;
+    if (nparams == 0) {
+        PLK_TRY(gate_dense(gate, K, inv, 0.0, U));
+        std::copy(U.begin(), U.end(), A.begin());
+        return PLK_OK;
+    }
+    static const double th[5] = {0.37, 1.61, 2.83, 4.07, 5.51};
+    double F[5][5];
+    std::vector<std::vector<double2>> R(5);
+    for (int k = 0; k < 5; k++) {
+        trig5(th[k], F[k]);
+        PLK_TRY(gate_dense(gate, K, inv, th[k], R[k]));
+    }
+    // Gaussian elimination with partial pivoting on F, applied to every entry
+    int perm[5] = {0, 1, 2, 3, 4};
+    for (int c = 0; c < 5; c++) {
+        int piv = c;
+        for (int r = c + 1; r < 5; r++)
+            if (std::fabs(F[r][c]) > std::fabs(F[piv][c])) piv = r;
+        if (piv != c) {
+            for (int j = 0; j < 5; j++) std::swap(F[c][j], F[piv][j]);
+            std::swap(R[c], R[piv]);
+            std::swap(perm[c], perm[piv]);
+        }
+        for (int r = c + 1; r < 5; r++) {
+            const double f = F[r][c] / F[c][c];
+            for (int j = c; j < 5; j++) F[r][j] -= f * F[c][j];
+            for (size_t e = 0; e < DD; e++) {
+                R[r][e].x -= f * R[c][e].x;
+                R[r][e].y -= f * R[c][e].y;
+            }
+        }
+    }
+    for (int i = 4; i >= 0; i--) {
+        for (size_t e = 0; e < DD; e++) {
+            double re = R[i][e].x, im = R[i][e].y;
+            for (int j = i + 1; j < 5; j++) {
+                re -= F[i][j] * A[j * DD + e].x;
+                im -= F[i][j] * A[j * DD + e].y;
+            }
+            A[i * DD + e] = mk<double2>(re / F[i][i], im / F[i][i]);
+        }
+    }
+    for (auto &z : A) {
+        if (std::fabs(z.x) < 1e-15) z.x = 0.0;
+        if (std::fabs(z.y) < 1e-15) z.y = 0.0;
+    }
+    // check the fit at angles it was not fitted on
+    for (double t : {0.9, 3.3, -2.2}) {
+        double f[5];
+        trig5(t, f);
+        PLK_TRY(gate_dense(gate, K, inv, t, U));
+        for (size_t e = 0; e < DD; e++) {
+            double re = 0, im = 0;
+            for (int i = 0; i < 5; i++) {
+                re += f[i] * A[i * DD + e].x;
+                im += f[i] * A[i * DD + e].y;
+            }
+            if (std::fabs(re - U[e].x) > 1e-12 || std::fabs(im - U[e].y) > 1e-12)
+                PLK_FAIL(PLK_ERR_UNSUPPORTED, "internal: gate matrix is not of degree one in theta/2");
+        }
+    }
+    return PLK_OK;
+}
+
+// -------------------------------------------------------- host structures --
+struct EPrep {
+    int32_t basis; // complex offset of the 5 coefficient blocks
+    int32_t pidx;  // flat parameter index, -1 for constant ops
+    int32_t out;   // complex offset of the output in the matrix buffer
+    uint8_t K, kind, conjT, pad;
+    uint8_t perm[4]; // DENSE: canonical bit of wires[j]
+};
+
+struct XOp { // an op after expansion (Rot -> RZ RY RZ)
+    int gate;
+    int K;
+    int wires[4];
+    std::vector<int> mrz_wires; // MultiRZ
+    bool inv;
+    int pidx;   // flat parameter index in the batch, -1 if none
+    int slot;   // Jacobian slot in the circuit, -1 if not trainable
+    int kind;   // EK_*
+    int basis;  // basis offset (complex)
+    int user_matrix; // index into the batch's user matrices, -1 if none
+};
+
+struct BatchConfig {
+    int cluster = 8;        // CTAs per cluster for the largest circuits
+    int threads = 256;      // threads per CTA
+    int smem_bits = 13;     // circuits with at most this many qubits stay in shared memory
+    int cluster_min_qubits = 17; // circuits with at least this many qubits go to clusters
+};
+
+struct LaunchPlan {
+    int grid = 0;
+    int cluster = 1;
+    size_t smem = 0;
+    std::vector<int32_t> order; // [order_cl..., order_solo...]
+    int n_cl = 0, n_solo = 0;
+    uint64_t slot_amps = 0;
+    int max_global_nq = 0;
+};
+
+} // namespace plk
+
+struct plk_batch_s {
+    int dtype = PLK_C64;
+    int device = 0;
+    // circuits as added
+    struct Circ {
+        int nq;
+        std::vector<plk::XOp> ops;
+        int p0, np;        // flat parameter range
+        int jac0, ntp;
+        std::vector<plk::ETerm> terms;
+    };
+    std::vector<Circ> circs;
+    std::vector<double> params; // flat initial parameters
+    std::vector<std::vector<double2>> user_mats;
+    std::map<int, int> basis_of;      // (gate * 2 + inv) -> basis offset
+    std::vector<double2> basis;       // host copy of all coefficient blocks
+    int njac = 0;
+    plk::BatchConfig cfg;
+    bool tuned = false;
+    // compiled
+    bool compiled = false;
+    std::vector<plk::ECirc> h_circ;
+    std::vector<plk::EWin> h_win;
+    std::vector<plk::EOp> h_ops;
+    std::vector<plk::ETrain> h_train;
+    std::vector<plk::ETerm> h_terms;
+    std::vector<plk::EPrep> h_prep;
+    std::vector<double2> h_gen; // constant generator blocks (appended after the prepared matrices)
+    int64_t n_mats = 0;         // prepared complex entries
+    std::vector<double> cost;
+    int max_nq = 0;
+    // device
+    void *d_circ = nullptr, *d_win = nullptr, *d_ops = nullptr, *d_train = nullptr, *d_terms = nullptr;
+    void *d_prep = nullptr, *d_basis = nullptr, *d_mats = nullptr, *d_order = nullptr;
+    double *d_params = nullptr, *d_expval = nullptr, *d_jac = nullptr, *d_jac_part = nullptr, *d_ev_part = nullptr;
+    unsigned *d_counters = nullptr;
+    void *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    double *h_params_pinned = nullptr, *h_out_pinned = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    bool use_graph = true;
+    int graph_cfg_key = -1;
+    plk::LaunchPlan lp;      // launch plan of the configuration lp_key
+    int lp_key = -1;
+    float last_ms = 0.0f;
+    long long last_launches = 0;
+};
+
+namespace plk {
+
+static bool is_diag_gate(int g) {
+    switch (g) {
+    case PLK_GATE_PAULIZ: case PLK_GATE_S: case PLK_GATE_T: case PLK_GATE_PHASESHIFT: case PLK_GATE_RZ:
+    case PLK_GATE_CZ: case PLK_GATE_CONTROLLEDPHASESHIFT: case PLK_GATE_CRZ: case PLK_GATE_ISINGZZ:
+        return true;
+    default: return false;
+    }
+}
+
+static int gate_nwires(int g);
+static int gate_nparams(int g);
+
+static int basis_for(plk_batch b, int gate, bool inv, int K, int &off) {
+    const int key = gate * 2 + (inv ? 1 : 0);
+    auto it = b->basis_of.find(key);
+    if (it != b->basis_of.end()) {
+        off = it->second;
+        return PLK_OK;
+    }
+    std::vector<double2> A;
+    const int Kb = gate == PLK_GATE_MULTIRZ ? 1 : K;
+    PLK_TRY(fit_gate(gate, Kb, inv, gate_nparams(gate), A));
+    off = (int)b->basis.size();
+    b->basis.insert(b->basis.end(), A.begin(), A.end());
+    b->basis_of[key] = off;
+    return PLK_OK;
+}
+
+static void free_device(plk_batch b) {
+    void **ptrs[] = {&b->d_circ, &b->d_win, &b->d_ops, &b->d_train, &b->d_terms, &b->d_prep, &b->d_basis,
+                     &b->d_mats, &b->d_order, (void **)&b->d_params, (void **)&b->d_expval, (void **)&b->d_jac,
+                     (void **)&b->d_jac_part, (void **)&b->d_ev_part, (void **)&b->d_counters, &b->d_scratch};
+    for (void **p : ptrs) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
+    b->scratch_bytes = 0;
+    if (b->h_params_pinned) cudaFreeHost(b->h_params_pinned);
+    if (b->h_out_pinned) cudaFreeHost(b->h_out_pinned);
+    b->h_params_pinned = b->h_out_pinned = nullptr;
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->graph_cfg_key = -1;
+    b->lp_key = -1;
+}
+
+// ----------------------------------------------------------- compilation --
+struct WinBuilder {
+    plk_batch b;
+    int nq;
+    bool bwd;
+    std::vector<EWin> &wins;
+    std::vector<EOp> &ops;
+    std::vector<ETrain> &train;
+    std::vector<EPrep> &prep;
+    std::vector<double2> &gen;
+    int64_t &n_mats;
+
+    std::vector<const XOp *> cur;
+    uint32_t wbits = 0; // state bits of the open window
+    int ntrain = 0;
+
+    static int popc(uint32_t x) { return __builtin_popcount(x); }
+
+    uint32_t need(const XOp &o) const {
+        if (o.kind == EK_DIAG || o.kind == EK_PARITY) return 0;
+        uint32_t m = 0;
+        for (int j = 0; j < o.K; j++) m |= 1u << (nq - 1 - o.wires[j]);
+        return m;
+    }
+
+    int add(const XOp &o) {
+        const uint32_t m = need(o);
+        const bool tr = bwd && o.slot >= 0;
+        if (!cur.empty() && (popc(wbits | m) > kWinBits || (int)cur.size() >= kMaxWinOps ||
+                             (tr && ntrain >= kMaxWinTrain)))
+            PLK_TRY(close());
+        cur.push_back(&o);
+        wbits |= m;
+        if (tr) ntrain++;
+        return PLK_OK;
+    }
+
+    int close() {
+        if (cur.empty()) return PLK_OK;
+        // pad with the highest unused state bits (low bits stay with the
+        // threads, which keeps global accesses coalesced)
+        uint32_t w = wbits;
+        for (int bit = nq - 1; bit >= 0 && popc(w) < kWinBits; bit--) w |= 1u << bit;
+        EWin win;
+        int r = 0;
+        int pos[32];
+        for (int bit = 0; bit < nq; bit++)
+            if (w >> bit & 1) {
+                win.rb[r] = (uint8_t)bit;
+                pos[bit] = r++;
+            }
+        win.op0 = (int)ops.size();
+        win.nops = (int)cur.size();
+        win.tr0 = (int)train.size();
+        win.ntrain = 0;
+        for (const XOp *op : cur) {
+            const XOp &o = *op;
+            EOp e;
+            std::memset(&e, 0, sizeof(e));
+            e.kind = (uint8_t)o.kind;
+            e.K = (uint8_t)o.K;
+            e.red = 0xff;
+            e.mat = -1;
+            e.gen = -1;
+            const int D = 1 << o.K;
+            uint8_t perm[4] = {0, 0, 0, 0};
+            if (o.kind == EK_CX) {
+                const int rc = pos[nq - 1 - o.wires[0]], rt = pos[nq - 1 - o.wires[1]];
+                e.sel = (uint8_t)(rc * 4 + rt);
+            } else if (o.kind == EK_DENSE) {
+                int rr[4], srt[4];
+                for (int j = 0; j < o.K; j++) srt[j] = rr[j] = pos[nq - 1 - o.wires[j]];
+                std::sort(srt, srt + o.K);
+                for (int j = 0; j < o.K; j++) perm[j] = (uint8_t)(std::find(srt, srt + o.K, rr[j]) - srt);
+                if (o.K == 1) {
+                    const int form = o.gate == PLK_GATE_RX ? EF_RX : (o.gate == PLK_GATE_RY ? EF_RY : EF_GENERAL);
+                    e.sel = (uint8_t)(srt[0] + 4 * form);
+                }
+                else if (o.K == 2) {
+                    static const int a[6] = {0, 0, 0, 1, 1, 2}, c[6] = {1, 2, 3, 2, 3, 3};
+                    for (int s = 0; s < 6; s++)
+                        if (a[s] == srt[0] && c[s] == srt[1]) e.sel = (uint8_t)s;
+                } else if (o.K == 3) {
+                    e.sel = (uint8_t)(6 - srt[0] - srt[1] - srt[2]);
+                } else {
+                    e.sel = 0;
+                }
+            } else if (o.kind == EK_DIAG) {
+                uint32_t bits = 0;
+                for (int j = 0; j < o.K; j++) bits |= (uint32_t)(nq - 1 - o.wires[j]) << (5 * j);
+                e.bits = bits;
+            } else { // parity
+                uint32_t mask = 0;
+                for (int wv : o.mrz_wires) mask |= 1u << (nq - 1 - wv);
+                e.bits = mask;
+            }
+            if (o.kind != EK_CX) {
+                EPrep p;
+                std::memset(&p, 0, sizeof(p));
+                p.basis = o.basis;
+                p.pidx = o.pidx;
+                p.out = (int32_t)n_mats;
+                p.K = (uint8_t)(o.kind == EK_PARITY ? 1 : o.K);
+                p.kind = (uint8_t)o.kind;
+                p.conjT = bwd ? 1 : 0;
+                std::memcpy(p.perm, perm, 4);
+                prep.push_back(p);
+                e.mat = (int32_t)n_mats;
+                n_mats += o.kind == EK_DENSE ? (int64_t)D * D : (o.kind == EK_DIAG ? D : 2);
+            }
+            if (bwd && o.slot >= 0) {
+                // generator (constant): canonical dense block or diagonal
+                GatePlan gp;
+                PLK_TRY(plan_generator(o.gate, o.kind == EK_PARITY ? (int)o.mrz_wires.size() : o.K, gp));
+                float gscale = (float)(-2.0 * gp.scale * (o.inv ? -1.0 : 1.0));
+                if (o.kind != EK_PARITY) {
+                    std::vector<double2> G;
+                    plan_dense(gp, o.K, G);
+                    e.gen = (int32_t)gen.size();
+                    if (o.kind == EK_DENSE && o.K == 1) {
+                        // monomial pattern (rows of G in canonical order = gate order for one wire)
+                        uint32_t pat = 0;
+                        for (int r2 = 0; r2 < 2; r2++)
+                            for (int c2 = 0; c2 < 2; c2++) {
+                                const double2 z = G[(size_t)r2 * 2 + c2];
+                                if (z.x == 0.0 && z.y == 0.0) continue;
+                                const int q = z.x == 1.0 ? 0 : z.y == 1.0 ? 1 : z.x == -1.0 ? 2 : z.y == -1.0 ? 3 : -1;
+                                if (q < 0 || (pat >> (4 * r2) & 1u))
+                                    PLK_FAIL(PLK_ERR_UNSUPPORTED, "internal: generator is not a signed permutation");
+                                pat |= (uint32_t)(1 | (c2 << 1) | (q << 2)) << (4 * r2);
+                            }
+                        e.bits = pat;
+                    }
+                    if (o.kind == EK_DENSE) {
+                        for (int r2 = 0; r2 < D; r2++)
+                            for (int c2 = 0; c2 < D; c2++) {
+                                int gr = 0, gc = 0;
+                                for (int j = 0; j < o.K; j++) {
+                                    gr |= ((r2 >> perm[j]) & 1) << (o.K - 1 - j);
+                                    gc |= ((c2 >> perm[j]) & 1) << (o.K - 1 - j);
+                                }
+                                gen.push_back(G[(size_t)gr * D + gc]);
+                            }
+                    } else { // diagonal generator
+                        for (int i = 0; i < D; i++) gen.push_back(G[(size_t)i * D + i]);
+                    }
+                }
+                e.red = (uint8_t)win.ntrain;
+                train.push_back(ETrain{o.slot, gscale});
+                win.ntrain++;
+            }
+            ops.push_back(e);
+        }
+        wins.push_back(win);
+        cur.clear();
+        wbits = 0;
+        ntrain = 0;
+        return PLK_OK;
+    }
+};
+
+static int compile_batch(plk_batch b) {
+    b->h_circ.clear();
+    b->h_win.clear();
+    b->h_ops.clear();
+    b->h_train.clear();
+    b->h_terms.clear();
+    b->h_prep.clear();
+    b->h_gen.clear();
+    b->cost.clear();
+    b->n_mats = 0;
+    b->max_nq = 0;
+    for (size_t ci = 0; ci < b->circs.size(); ci++) {
+        auto &c = b->circs[ci];
+        ECirc e;
+        e.nq = c.nq;
+        e.id = (int)ci;
+        e.jac0 = c.jac0;
+        e.ntp = c.ntp;
+        e.term0 = (int)b->h_terms.size();
+        e.nterms = (int)c.terms.size();
+        b->h_terms.insert(b->h_terms.end(), c.terms.begin(), c.terms.end());
+        for (int dir = 0; dir < 2; dir++) {
+            const bool bwd = dir == 1;
+            WinBuilder wb{b, c.nq, bwd, b->h_win, b->h_ops, b->h_train, b->h_prep, b->h_gen, b->n_mats};
+            const int w0 = (int)b->h_win.size();
+            const int n = (int)c.ops.size();
+            if (!bwd) {
+                for (int k = 0; k < n; k++) PLK_TRY(wb.add(c.ops[k]));
+            } else {
+                // ops before the first trainable op do not change the Jacobian
+                // (the reference loop ends there too, AdjointDiffKokkos.hpp:447)
+                int first = n;
+                for (int k = 0; k < n; k++)
+                    if (c.ops[k].slot >= 0) {
+                        first = k;
+                        break;
+                    }
+                for (int k = n - 1; k >= first; k--) PLK_TRY(wb.add(c.ops[k]));
+            }
+            PLK_TRY(wb.close());
+            if (!bwd) {
+                e.fw0 = w0;
+                e.nfw = (int)b->h_win.size() - w0;
+            } else {
+                e.bw0 = w0;
+                e.nbw = (int)b->h_win.size() - w0;
+            }
+        }
+        b->h_circ.push_back(e);
+        double work = 0;
+        for (int w = e.fw0; w < e.fw0 + e.nfw; w++) work += 4 + b->h_win[w].nops;
+        for (int w = e.bw0; w < e.bw0 + e.nbw; w++) work += 2 * (4 + b->h_win[w].nops);
+        work += 2 + e.nterms;
+        b->cost.push_back(work * std::ldexp(1.0, c.nq));
+        b->max_nq = std::max(b->max_nq, c.nq);
+    }
+    // generator blocks follow the prepared matrices in one buffer
+    for (auto &o : b->h_ops)
+        if (o.gen >= 0) o.gen += (int32_t)b->n_mats;
+    b->compiled = true;
+    return PLK_OK;
+}
+
+static int upload_vec(void **dptr, const void *src, size_t bytes, cudaStream_t st) {
+    if (*dptr) cudaFree(*dptr);
+    *dptr = nullptr;
+    PLK_CUDA(cudaMalloc(dptr, std::max<size_t>(bytes, 16)));
+    if (bytes) PLK_CUDA(cudaMemcpyAsync(*dptr, src, bytes, cudaMemcpyHostToDevice, st));
+    return PLK_OK;
+}
+
+template <class T> static int upload_batch(plk_batch b) {
+    using V = c2_t<T>;
+    free_device(b);
+    cudaStream_t st = b->stream;
+    PLK_TRY(upload_vec(&b->d_circ, b->h_circ.data(), b->h_circ.size() * sizeof(ECirc), st));
+    PLK_TRY(upload_vec(&b->d_win, b->h_win.data(), b->h_win.size() * sizeof(EWin), st));
+    PLK_TRY(upload_vec(&b->d_ops, b->h_ops.data(), b->h_ops.size() * sizeof(EOp), st));
+    PLK_TRY(upload_vec(&b->d_train, b->h_train.data(), b->h_train.size() * sizeof(ETrain), st));
+    PLK_TRY(upload_vec(&b->d_terms, b->h_terms.data(), b->h_terms.size() * sizeof(ETerm), st));
+    PLK_TRY(upload_vec(&b->d_prep, b->h_prep.data(), b->h_prep.size() * sizeof(EPrep), st));
+    PLK_TRY(upload_vec(&b->d_basis, b->basis.data(), b->basis.size() * sizeof(double2), st));
+    // matrices: prepared region then constant generators (cast to the state precision)
+    const size_t nm = (size_t)b->n_mats + b->h_gen.size();
+    std::vector<V> gen(b->h_gen.size());
+    for (size_t i = 0; i < gen.size(); i++) gen[i] = mk<V>((T)b->h_gen[i].x, (T)b->h_gen[i].y);
+    PLK_CUDA(cudaMalloc(&b->d_mats, std::max<size_t>(nm, 1) * sizeof(V)));
+    if (!gen.empty())
+        PLK_CUDA(cudaMemcpyAsync((V *)b->d_mats + b->n_mats, gen.data(), gen.size() * sizeof(V), cudaMemcpyHostToDevice,
+                                 st));
+    const size_t nc = b->circs.size();
+    PLK_CUDA(cudaMalloc(&b->d_order, std::max<size_t>(nc, 1) * 2 * sizeof(int32_t)));
+    PLK_CUDA(cudaMalloc(&b->d_params, std::max<size_t>(b->params.size(), 1) * sizeof(double)));
+    PLK_CUDA(cudaMemcpyAsync(b->d_params, b->params.data(), b->params.size() * sizeof(double), cudaMemcpyHostToDevice,
+                             st));
+    PLK_CUDA(cudaMalloc(&b->d_expval, std::max<size_t>(nc, 1) * sizeof(double)));
+    PLK_CUDA(cudaMalloc(&b->d_jac, std::max(b->njac, 1) * sizeof(double)));
+    PLK_CUDA(cudaMalloc(&b->d_jac_part, std::max(b->njac, 1) * kMaxCluster * sizeof(double)));
+    PLK_CUDA(cudaMalloc(&b->d_ev_part, std::max<size_t>(nc, 1) * kMaxCluster * sizeof(double)));
+    PLK_CUDA(cudaMalloc(&b->d_counters, 4 * sizeof(unsigned)));
+    PLK_CUDA(cudaMallocHost(&b->h_params_pinned, std::max<size_t>(b->params.size(), 1) * sizeof(double)));
+    PLK_CUDA(cudaMallocHost(&b->h_out_pinned, (nc + b->njac + 1) * sizeof(double)));
+    PLK_CUDA(cudaStreamSynchronize(st));
+    return PLK_OK;
+}
+
+// ------------------------------------------------------------- kernels --
+template <class T>
+__global__ void k_batch_prepare(const EPrep *__restrict__ prep, int nprep, const double2 *__restrict__ basis,
+                                const double *__restrict__ params, c2_t<T> *__restrict__ mats) {
+    using V = c2_t<T>;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nprep) return;
+    const EPrep p = prep[e];
+    double f[5] = {1.0, 0.0, 0.0, 0.0, 0.0};
+    if (p.pidx >= 0) {
+        const double th = params[p.pidx];
+        sincos(th * 0.5, &f[2], &f[1]);
+        sincos(th, &f[4], &f[3]);
+    }
+    const int K = p.K, D = 1 << K;
+    if (p.kind == EK_DENSE) {
+        const int DD = D * D;
+        for (int idx = 0; idx < DD; idx++) {
+            const int r = idx / D, c = idx % D;
+            int gr = 0, gc = 0;
+            for (int j = 0; j < K; j++) {
+                gr |= ((r >> p.perm[j]) & 1) << (K - 1 - j);
+                gc |= ((c >> p.perm[j]) & 1) << (K - 1 - j);
+            }
+            const int src = p.conjT ? gc * D + gr : gr * D + gc;
+            double re = 0.0, im = 0.0;
+            for (int i = 0; i < 5; i++) {
+                const double2 a = basis[p.basis + i * DD + src];
+                re = fma(f[i], a.x, re);
+                im = fma(f[i], a.y, im);
+            }
+            mats[p.out + idx] = mk<V>((T)re, (T)(p.conjT ? -im : im));
+        }
+    } else { // diagonal (DIAG: 2^K entries; PARITY: the 2 entries of MultiRZ on one wire)
+        const int DD = D * D;
+        for (int i2 = 0; i2 < D; i2++) {
+            double re = 0.0, im = 0.0;
+            for (int i = 0; i < 5; i++) {
+                const double2 a = basis[p.basis + i * DD + i2 * D + i2];
+                re = fma(f[i], a.x, re);
+                im = fma(f[i], a.y, im);
+            }
+            mats[p.out + i2] = mk<V>((T)re, (T)(p.conjT ? -im : im));
+        }
+    }
+}
+
+// C > 1 only for global states shared by a cluster
+__device__ __forceinline__ void esync(int C) {
+    if (C > 1) {
+        __threadfence();
+        cg::this_cluster().sync();
+    } else {
+        __syncthreads();
+    }
+}
+
+template <class T, bool BWD>
+__device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps], c2_t<T> (&hv)[kWinAmps], uint64_t base,
+                                          const uint64_t (&bb)[4], const c2_t<T> *__restrict__ mats, EAcc<T> &acc,
+                                          EAcc<T> &acc1) {
+    using V = c2_t<T>;
+    const bool tr = BWD && op.red != 0xff;
+    if (op.kind == EK_DENSE) {
+        const V *U = mats + op.mat;
+#define PLK_DENSE1_CASE(S_)                                                                                           \
+    case 16 + S_:                                                                                                      \
+        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
+        dense_apply<1, S_>(lv, U);                                                                                     \
+        if (BWD) dense_apply<1, S_>(hv, U);                                                                            \
+        break;                                                                                                         \
+    case 16 + 4 + S_:                                                                                                  \
+        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
+        rx_apply<S_>(lv, U);                                                                                           \
+        if (BWD) rx_apply<S_>(hv, U);                                                                                  \
+        break;                                                                                                         \
+    case 16 + 8 + S_:                                                                                                  \
+        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
+        ry_apply<S_>(lv, U);                                                                                           \
+        if (BWD) ry_apply<S_>(hv, U);                                                                                  \
+        break;
+#define PLK_DENSE_CASE(K_, S_)                                                                                        \
+    case K_ * 16 + S_:                                                                                                 \
+        if (tr) dense_gen_dot<K_, S_, T>(lv, hv, mats + op.gen, acc);                                                  \
+        dense_apply<K_, S_>(lv, U);                                                                                    \
+        if (BWD) dense_apply<K_, S_>(hv, U);                                                                           \
+        break;
+        switch (op.K * 16 + op.sel) {
+            PLK_DENSE1_CASE(0) PLK_DENSE1_CASE(1) PLK_DENSE1_CASE(2) PLK_DENSE1_CASE(3)
+            PLK_DENSE_CASE(2, 0) PLK_DENSE_CASE(2, 1) PLK_DENSE_CASE(2, 2) PLK_DENSE_CASE(2, 3)
+            PLK_DENSE_CASE(2, 4) PLK_DENSE_CASE(2, 5)
+        default: {
+            // K = 3, 4: sel = missing register bit (K = 3) or 0 (K = 4)
+            // (copies keep lv / hv themselves in registers)
+            const uint32_t smask = op.K == 4 ? 15u : (15u & ~(1u << op.sel));
+            V tl[kWinAmps], th[kWinAmps];
+#pragma unroll
+            for (int j = 0; j < kWinAmps; j++) {
+                tl[j] = lv[j];
+                th[j] = hv[j];
+            }
+            if (tr) dense_gen_dot_rt<T>(tl, th, mats + op.gen, op.K, smask, acc);
+            dense_apply_rt(tl, U, op.K, smask);
+            if (BWD) dense_apply_rt(th, U, op.K, smask);
+#pragma unroll
+            for (int j = 0; j < kWinAmps; j++) {
+                lv[j] = tl[j];
+                hv[j] = th[j];
+            }
+            break;
+        }
+        }
+#undef PLK_DENSE_CASE
+#undef PLK_DENSE1_CASE
+    } else if (op.kind == EK_CX) {
+#define PLK_CX_CASE(C_, T_)                                                                                           \
+    case C_ * 4 + T_:                                                                                                  \
+        cx_apply<C_, T_>(lv);                                                                                          \
+        if (BWD) cx_apply<C_, T_>(hv);                                                                                 \
+        break;
+        switch (op.sel) {
+            PLK_CX_CASE(0, 1) PLK_CX_CASE(0, 2) PLK_CX_CASE(0, 3) PLK_CX_CASE(1, 0) PLK_CX_CASE(1, 2)
+            PLK_CX_CASE(1, 3) PLK_CX_CASE(2, 0) PLK_CX_CASE(2, 1) PLK_CX_CASE(2, 3) PLK_CX_CASE(3, 0)
+            PLK_CX_CASE(3, 1) PLK_CX_CASE(3, 2)
+        default: break;
+        }
+#undef PLK_CX_CASE
+    } else if (op.kind == EK_DIAG && op.K == 1) {
+        // one-wire diagonal (RZ, PhaseShift, Z, S, T): two phases by one bit
+        const uint32_t b0 = op.bits & 31u;
+        const V e0 = mats[op.mat], e1 = mats[op.mat + 1];
+        T g0 = 0, g1 = 0;
+        if (tr) {
+            g0 = mats[op.gen].x;
+            g1 = mats[op.gen + 1].x;
+        }
+        T t = 0;
+#pragma unroll
+        for (int j = 0; j < kWinAmps; j++) {
+            const uint64_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                 ((j & 8) ? bb[3] : 0);
+            const bool one = (idx >> b0) & 1u;
+            if (tr) {
+                // Im(conj(h) g v) = g (h.x v.y - h.y v.x); two amplitudes per FP32 partial
+                const T gd = one ? g1 : g0;
+                t = fma(gd * hv[j].x, lv[j].y, t);
+                t = fma(-gd * hv[j].y, lv[j].x, t);
+                if (j & 1) {
+                    ((j >> 1) & 1 ? acc1 : acc).addf(t);
+                    t = 0;
+                }
+            }
+            const V e = one ? e1 : e0;
+            lv[j] = cmul(lv[j], e);
+            if (BWD) hv[j] = cmul(hv[j], e);
+        }
+    } else {
+        const bool parity = op.kind == EK_PARITY;
+#pragma unroll
+        for (int j = 0; j < kWinAmps; j++) {
+            const uint64_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                 ((j & 8) ? bb[3] : 0);
+            const uint32_t g = parity ? (uint32_t)(__popcll(idx & (uint64_t)op.bits) & 1) : diag_index(idx, op.bits, op.K);
+            const V e = mats[op.mat + g];
+            if (tr) {
+                // generator diagonal: MultiRZ (-1)^parity, otherwise real entries 0, +-1
+                const T gd = parity ? (g ? (T)-1 : (T)1) : mats[op.gen + g].x;
+                (j & 1 ? acc1 : acc).im_dot(hv[j], mk<V>(gd * lv[j].x, gd * lv[j].y));
+            }
+            lv[j] = cmul(lv[j], e);
+            if (BWD) hv[j] = cmul(hv[j], e);
+        }
+    }
+}
+
+template <class T, int NT, int MODE, bool BWD>
+__device__ __noinline__ void run_window(const EngArgs<T> &a, const EWin &w, int nq, c2_t<T> *lam, c2_t<T> *hl, uint64_t t0,
+                                        uint64_t tstep, typename EAcc<T>::Slot *part) {
+    using V = c2_t<T>;
+    const int lane = threadIdx.x & 31;
+    const uint64_t nu = 1ull << (nq - kWinBits);
+    const uint64_t bb[4] = {1ull << w.rb[0], 1ull << w.rb[1], 1ull << w.rb[2], 1ull << w.rb[3]};
+    for (uint64_t u = t0; u - lane < nu; u += tstep) {
+        const bool act = u < nu;
+        uint64_t base = u;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint64_t lo = base & (bb[i] - 1);
+            base = ((base ^ lo) << 1) | lo;
+        }
+        V lv[kWinAmps], hv[kWinAmps];
+#pragma unroll
+        for (int j = 0; j < kWinAmps; j++) {
+            const uint64_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                 ((j & 8) ? bb[3] : 0);
+            lv[j] = act ? eld<T, MODE>(lam, idx) : mk<V>(0, 0);
+            if (BWD) hv[j] = act ? eld<T, MODE>(hl, idx) : mk<V>(0, 0);
+            else hv[j] = mk<V>(0, 0);
+        }
+        for (int k = 0; k < w.nops; k++) {
+            const EOp op = a.ops[w.op0 + k];
+            EAcc<T> acc, acc1;
+            if (BWD && op.red != 0xff) acc.load(part[op.red * NT + threadIdx.x]);
+            window_op<T, BWD>(op, lv, hv, base, bb, a.mats, acc, acc1);
+            if (BWD && op.red != 0xff) {
+                acc.merge(acc1);
+                part[op.red * NT + threadIdx.x] = acc.slot();
+            }
+        }
+        if (act) {
+#pragma unroll
+            for (int j = 0; j < kWinAmps; j++) {
+                const uint64_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                     ((j & 8) ? bb[3] : 0);
+                est<T, MODE>(lam, idx, lv[j]);
+                if (BWD) est<T, MODE>(hl, idx, hv[j]);
+            }
+        }
+    }
+}
+
+// Per trainable op of the window: one warp sums the CTA's per-thread partials
+// in a fixed order (and clears them for the next use of the buffer).
+template <class T, int NT>
+__device__ void finalize_window(const EngArgs<T> &a, const ECirc &ci, const EWin &w, typename EAcc<T>::Slot *part,
+                                int rank, int C) {
+    constexpr int NW = NT / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int t = warp; t < w.ntrain; t += NW) {
+        EAcc<T> acc;
+#pragma unroll
+        for (int i = 0; i < NT / 32; i++) {
+            auto &sl = part[t * NT + i * 32 + lane];
+            EAcc<T> x;
+            x.load(sl);
+            acc.merge(x);
+            sl = typename EAcc<T>::Slot{};
+        }
+        const double s = acc.warp_sum();
+        if (lane == 0) {
+            const ETrain tr = a.train[w.tr0 + t];
+            const int js = ci.jac0 + tr.slot;
+            if (C > 1) a.jac_part[(size_t)js * kMaxCluster + rank] = (double)tr.gscale * s;
+            else a.jac[js] = (double)tr.gscale * s;
+        }
+    }
+}
+
+// H lambda and <lambda|H|lambda>; H = sum_w c_w P_w with
+// <i|P|lambda> = i^ny (-1)^popc((i ^ x) & z) lambda[i ^ x]
+template <class T, int NT, int MODE>
+__device__ void h_pass(const EngArgs<T> &a, const ECirc &ci, c2_t<T> *lam, c2_t<T> *hl, uint64_t t0, uint64_t tstep,
+                       double *misc, int rank, int C) {
+    using V = c2_t<T>;
+    constexpr int NW = NT / 32;
+    const uint64_t N = 1ull << ci.nq;
+    EAcc<T> acc;
+    for (uint64_t i = t0; i < N; i += tstep) {
+        const V li = eld<T, MODE>(lam, i);
+        V hs = mk<V>(0, 0);
+        for (int k = 0; k < ci.nterms; k++) {
+            const ETerm tm = a.terms[ci.term0 + k];
+            const uint64_t j = i ^ (uint64_t)tm.x;
+            const V v = eld<T, MODE>(lam, j);
+            const int q = (tm.ny + 2 * (__popcll(j & (uint64_t)tm.z) & 1)) & 3;
+            const V u = q == 0 ? v : (q == 1 ? mul_i(v) : (q == 2 ? cneg(v) : mul_mi(v)));
+            const T c = (T)tm.c;
+            hs = mk<V>(hs.x + c * u.x, hs.y + c * u.y);
+            if constexpr (sizeof(T) == 4) acc.re_dot_scaled(tm.ch, tm.cl, li, u);
+            else acc.re_dot_c(tm.c, li, u);
+        }
+        est<T, MODE>(hl, i, hs);
+    }
+    const double s = acc.warp_sum();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) misc[warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int wp = 0; wp < NW; wp++) t += misc[wp];
+        if (C > 1) a.ev_part[(size_t)ci.id * kMaxCluster + rank] = t;
+        else a.expval[ci.id] = t;
+    }
+}
+
+template <class T, int NT, int MODE>
+__device__ void run_circuit(const EngArgs<T> &a, int cid, int rank, int C, c2_t<T> *lam, c2_t<T> *hl,
+                            typename EAcc<T>::Slot *part, double *misc) {
+    using V = c2_t<T>;
+    constexpr int NW = NT / 32;
+    const ECirc ci = a.circ[cid];
+    const uint64_t N = 1ull << ci.nq;
+    const uint64_t t0 = (uint64_t)rank * NT + threadIdx.x, tstep = (uint64_t)C * NT;
+    for (uint64_t i = t0; i < N; i += tstep) est<T, MODE>(lam, i, mk<V>(i == 0 ? (T)1 : (T)0, (T)0));
+    esync(C);
+    for (int k = 0; k < ci.nfw; k++) {
+        const EWin w = a.win[ci.fw0 + k];
+        run_window<T, NT, MODE, false>(a, w, ci.nq, lam, hl, t0, tstep, part);
+        esync(C);
+    }
+    h_pass<T, NT, MODE>(a, ci, lam, hl, t0, tstep, misc, rank, C);
+    esync(C);
+    if (C > 1 && rank == 0 && threadIdx.x == 0) {
+        double t = 0.0;
+        for (int r = 0; r < C; r++) t += a.ev_part[(size_t)ci.id * kMaxCluster + r];
+        a.expval[ci.id] = t;
+    }
+    for (int k = 0; k < ci.nbw; k++) {
+        const EWin w = a.win[ci.bw0 + k];
+        typename EAcc<T>::Slot *rb = part + (k & 1) * kMaxWinTrain * NT;
+        run_window<T, NT, MODE, true>(a, w, ci.nq, lam, hl, t0, tstep, rb);
+        esync(C);
+        finalize_window<T, NT>(a, ci, w, rb, rank, C);
+    }
+    esync(C);
+    if (C > 1 && rank == 0) {
+        for (int s = threadIdx.x; s < ci.ntp; s += NT) {
+            double t = 0.0;
+            for (int r = 0; r < C; r++) t += a.jac_part[(size_t)(ci.jac0 + s) * kMaxCluster + r];
+            a.jac[ci.jac0 + s] = t;
+        }
+    }
+}
+
+template <class T, int NT>
+__global__ void __launch_bounds__(NT, 1) k_batch_engine(const EngArgs<T> a) {
+    using V = c2_t<T>;
+    constexpr int NW = NT / 32;
+    extern __shared__ __align__(16) unsigned char esmem[];
+    V *s_lam = (V *)esmem;
+    V *s_hl = s_lam + (1u << a.smem_bits);
+    using Slot = typename EAcc<T>::Slot;
+    Slot *s_part = (Slot *)(s_hl + (1u << a.smem_bits)); // [2][kMaxWinTrain][NT]
+    double *s_misc = (double *)(s_part + 2 * kMaxWinTrain * NT);
+    __shared__ int s_cur;
+    for (int i = threadIdx.x; i < 2 * kMaxWinTrain * NT; i += NT) s_part[i] = Slot{};
+    __syncthreads();
+    V *slot_cta = a.scratch ? a.scratch + (uint64_t)blockIdx.x * 2 * a.slot_amps : nullptr;
+    if (a.n_cl > 0) {
+        cg::cluster_group cl = cg::this_cluster();
+        const int C = (int)cl.num_blocks();
+        const int rank = (int)cl.block_rank();
+        V *slot_cl = a.scratch + (uint64_t)(blockIdx.x - rank) * 2 * a.slot_amps;
+        for (;;) {
+            if (rank == 0 && threadIdx.x == 0) s_cur = (int)atomicAdd(&a.counters[0], 1u);
+            cl.sync();
+            const int c = *cl.map_shared_rank(&s_cur, 0);
+            cl.sync();
+            if (c >= a.n_cl) break;
+            run_circuit<T, NT, EM_GLOBAL>(a, a.order_cl[c], rank, C, slot_cl, slot_cl + a.slot_amps, s_part, s_misc);
+        }
+    }
+    for (;;) {
+        if (threadIdx.x == 0) s_cur = (int)atomicAdd(&a.counters[1], 1u);
+        __syncthreads();
+        const int c = s_cur;
+        __syncthreads();
+        if (c >= a.n_solo) break;
+        const int cid = a.order_solo[c];
+        if (a.circ[cid].nq <= a.smem_bits) run_circuit<T, NT, EM_SMEM>(a, cid, 0, 1, s_lam, s_hl, s_part, s_misc);
+        else run_circuit<T, NT, EM_GLOBAL>(a, cid, 0, 1, slot_cta, slot_cta + a.slot_amps, s_part, s_misc);
+    }
+}
+
+// ------------------------------------------------------------- launching --
+template <class T, int NT> static size_t engine_smem(int smem_bits) {
+    return 2 * (sizeof(c2_t<T>) << smem_bits) + 2 * kMaxWinTrain * NT * sizeof(typename EAcc<T>::Slot) +
+           (NT / 32 + 8) * sizeof(double);
+}
+
+template <class T, int NT> static int plan_launch(plk_batch b, LaunchPlan &lp) {
+    const BatchConfig &cfg = b->cfg;
+    const int maxsb = sizeof(T) == 4 ? 13 : 12;
+    const int sb = std::min(cfg.smem_bits, maxsb);
+    lp.smem = engine_smem<T, NT>(sb);
+    auto kern = k_batch_engine<T, NT>;
+    PLK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lp.smem));
+    DeviceCtx *d = nullptr;
+    PLK_TRY(device_ctx(b->device, &d));
+    int per_sm = 0;
+    PLK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, lp.smem));
+    if (per_sm < 1) PLK_FAIL(PLK_ERR_UNSUPPORTED, "batch engine does not fit on an SM with this configuration");
+    lp.cluster = std::max(1, std::min(cfg.cluster, kMaxCluster));
+    // classify and order circuits (largest cost first)
+    std::vector<int32_t> cl, solo;
+    lp.max_global_nq = 0;
+    for (size_t i = 0; i < b->h_circ.size(); i++) {
+        const int nq = b->h_circ[i].nq;
+        if (lp.cluster > 1 && nq > sb && nq >= cfg.cluster_min_qubits) cl.push_back((int32_t)i);
+        else solo.push_back((int32_t)i);
+        if (nq > sb) lp.max_global_nq = std::max(lp.max_global_nq, nq);
+    }
+    auto by_cost = [&](int32_t x, int32_t y) { return b->cost[x] > b->cost[y] || (b->cost[x] == b->cost[y] && x < y); };
+    std::sort(cl.begin(), cl.end(), by_cost);
+    std::sort(solo.begin(), solo.end(), by_cost);
+    if (cl.empty()) lp.cluster = 1;
+    lp.n_cl = (int)cl.size();
+    lp.n_solo = (int)solo.size();
+    lp.order = cl;
+    lp.order.insert(lp.order.end(), solo.begin(), solo.end());
+    if (lp.cluster > 1) {
+        cudaLaunchConfig_t lc = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = lp.cluster;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        lc.gridDim = dim3(lp.cluster * d->sm_count);
+        lc.blockDim = dim3(NT);
+        lc.dynamicSmemBytes = lp.smem;
+        lc.attrs = at;
+        lc.numAttrs = 1;
+        int ncl = 0;
+        PLK_CUDA(cudaOccupancyMaxActiveClusters(&ncl, kern, &lc));
+        if (ncl < 1) PLK_FAIL(PLK_ERR_UNSUPPORTED, "no cluster of this size fits the device");
+        lp.grid = ncl * lp.cluster;
+    } else {
+        lp.grid = per_sm * d->sm_count;
+    }
+    lp.slot_amps = lp.max_global_nq > 0 ? (1ull << lp.max_global_nq) : 0;
+    return PLK_OK;
+}
+
+template <class T, int NT> static int launch_engine(plk_batch b, const LaunchPlan &lp, cudaStream_t st) {
+    using V = c2_t<T>;
+    EngArgs<T> a;
+    a.circ = (const ECirc *)b->d_circ;
+    a.win = (const EWin *)b->d_win;
+    a.ops = (const EOp *)b->d_ops;
+    a.train = (const ETrain *)b->d_train;
+    a.terms = (const ETerm *)b->d_terms;
+    a.mats = (const V *)b->d_mats;
+    a.order_cl = (const int32_t *)b->d_order;
+    a.order_solo = (const int32_t *)b->d_order + lp.n_cl;
+    a.n_cl = lp.n_cl;
+    a.n_solo = lp.n_solo;
+    a.counters = b->d_counters;
+    a.scratch = (V *)b->d_scratch;
+    a.slot_amps = lp.slot_amps;
+    a.expval = b->d_expval;
+    a.jac = b->d_jac;
+    a.jac_part = b->d_jac_part;
+    a.ev_part = b->d_ev_part;
+    a.smem_bits = std::min(b->cfg.smem_bits, sizeof(T) == 4 ? 13 : 12);
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute at[1];
+    lc.gridDim = dim3(lp.grid);
+    lc.blockDim = dim3(NT);
+    lc.dynamicSmemBytes = lp.smem;
+    lc.stream = st;
+    if (lp.cluster > 1) {
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = lp.cluster;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        lc.attrs = at;
+        lc.numAttrs = 1;
+    }
+    PLK_CUDA(cudaLaunchKernelEx(&lc, k_batch_engine<T, NT>, a));
+    return PLK_OK;
+}
+
+static int cfg_key(const BatchConfig &c) {
+    return ((c.cluster * 1024 + c.threads) * 64 + c.smem_bits) * 64 + c.cluster_min_qubits;
+}
+
+// 512-thread CTAs halve the register budget (128 per thread) and spill the
+// 32 window amplitudes; only 256-thread CTAs are built.
+constexpr bool kBuild512 = false;
+template <class T> static bool use512(const plk_batch b) { return sizeof(T) == 4 && b->cfg.threads == 512; }
+
+template <class T> static int prepare_run(plk_batch b) {
+    if (!b->compiled) {
+        PLK_TRY(compile_batch(b));
+        PLK_TRY(upload_batch<T>(b));
+    }
+    if (b->lp_key == cfg_key(b->cfg)) return PLK_OK;
+    LaunchPlan &lp = b->lp;
+    lp = LaunchPlan();
+    if constexpr (sizeof(T) == 4 && kBuild512) {
+        if (use512<T>(b)) PLK_TRY((plan_launch<T, 512>(b, lp)));
+        else PLK_TRY((plan_launch<T, 256>(b, lp)));
+    } else {
+        PLK_TRY((plan_launch<T, 256>(b, lp)));
+    }
+    // order and scratch for this configuration
+    PLK_CUDA(cudaMemcpyAsync(b->d_order, lp.order.data(), lp.order.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                             b->stream));
+    const size_t need = lp.slot_amps ? (size_t)lp.grid * 2 * lp.slot_amps * sizeof(c2_t<T>) : 0;
+    if (need > b->scratch_bytes) {
+        if (b->d_scratch) cudaFree(b->d_scratch);
+        b->d_scratch = nullptr;
+        b->scratch_bytes = 0;
+        PLK_CUDA(cudaMalloc(&b->d_scratch, need));
+        b->scratch_bytes = need;
+    }
+    PLK_CUDA(cudaStreamSynchronize(b->stream));
+    b->lp_key = cfg_key(b->cfg);
+    return PLK_OK;
+}
+
+// The stream work of one run: counters, matrices from parameters, engine.
+template <class T> static int enqueue_run(plk_batch b, const double *d_params, cudaStream_t st) {
+    const LaunchPlan &lp = b->lp;
+    PLK_CUDA(cudaMemsetAsync(b->d_counters, 0, 4 * sizeof(unsigned), st));
+    const int np = (int)b->h_prep.size();
+    if (np > 0) {
+        k_batch_prepare<T><<<(np + 255) / 256, 256, 0, st>>>((const EPrep *)b->d_prep, np, (const double2 *)b->d_basis,
+                                                             d_params, (c2_t<T> *)b->d_mats);
+        PLK_CHECK_LAUNCH();
+    }
+    if constexpr (sizeof(T) == 4 && kBuild512) {
+        if (use512<T>(b)) PLK_TRY((launch_engine<T, 512>(b, lp, st)));
+        else PLK_TRY((launch_engine<T, 256>(b, lp, st)));
+    } else {
+        PLK_TRY((launch_engine<T, 256>(b, lp, st)));
+    }
+    return PLK_OK;
+}
+
+template <class T> static int run_host(plk_batch b, double *expval, double *jac) {
+    PLK_TRY(prepare_run<T>(b));
+    const size_t nc = b->circs.size();
+    const size_t npar = b->params.size();
+    cudaStream_t st = b->stream;
+    std::memcpy(b->h_params_pinned, b->params.data(), npar * sizeof(double));
+    if (b->use_graph && b->graph_cfg_key != cfg_key(b->cfg)) {
+        if (b->graph) cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+        cudaGraph_t g = nullptr;
+        PLK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int rc = PLK_OK;
+        if (npar && cudaMemcpyAsync(b->d_params, b->h_params_pinned, npar * sizeof(double), cudaMemcpyHostToDevice,
+                                    st) != cudaSuccess)
+            rc = PLK_ERR_CUDA;
+        if (rc == PLK_OK) rc = enqueue_run<T>(b, b->d_params, st);
+        if (rc == PLK_OK && cudaMemcpyAsync(b->h_out_pinned, b->d_expval, nc * sizeof(double), cudaMemcpyDeviceToHost,
+                                            st) != cudaSuccess)
+            rc = PLK_ERR_CUDA;
+        if (rc == PLK_OK && b->njac &&
+            cudaMemcpyAsync(b->h_out_pinned + nc, b->d_jac, b->njac * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+                cudaSuccess)
+            rc = PLK_ERR_CUDA;
+        const cudaError_t ec = cudaStreamEndCapture(st, &g);
+        if (rc != PLK_OK) {
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            PLK_FAIL(rc, "batch: graph capture failed: " + last_error());
+        }
+        PLK_CUDA(ec);
+        const cudaError_t ei = cudaGraphInstantiate(&b->graph, g, 0);
+        cudaGraphDestroy(g);
+        PLK_CUDA(ei);
+        b->graph_cfg_key = cfg_key(b->cfg);
+    }
+    cudaEvent_t e0, e1;
+    PLK_CUDA(cudaEventCreate(&e0));
+    PLK_CUDA(cudaEventCreate(&e1));
+    PLK_CUDA(cudaEventRecord(e0, st));
+    if (b->use_graph) {
+        PLK_CUDA(cudaGraphLaunch(b->graph, st));
+    } else {
+        if (npar)
+            PLK_CUDA(cudaMemcpyAsync(b->d_params, b->h_params_pinned, npar * sizeof(double), cudaMemcpyHostToDevice, st));
+        PLK_TRY(enqueue_run<T>(b, b->d_params, st));
+        PLK_CUDA(cudaMemcpyAsync(b->h_out_pinned, b->d_expval, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
+        if (b->njac)
+            PLK_CUDA(cudaMemcpyAsync(b->h_out_pinned + nc, b->d_jac, b->njac * sizeof(double), cudaMemcpyDeviceToHost,
+                                     st));
+    }
+    PLK_CUDA(cudaEventRecord(e1, st));
+    PLK_CUDA(cudaStreamSynchronize(st));
+    cudaEventElapsedTime(&b->last_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->last_launches = b->h_prep.empty() ? 1 : 2;
+    if (expval) std::memcpy(expval, b->h_out_pinned, nc * sizeof(double));
+    if (jac && b->njac) std::memcpy(jac, b->h_out_pinned + nc, b->njac * sizeof(double));
+    return PLK_OK;
+}
+
+template <class T>
+static int run_device(plk_batch b, const double *d_params, double *d_expval, double *d_jac, cudaStream_t st) {
+    PLK_TRY(prepare_run<T>(b));
+    PLK_TRY(enqueue_run<T>(b, d_params ? d_params : b->d_params, st));
+    const size_t nc = b->circs.size();
+    if (d_expval)
+        PLK_CUDA(cudaMemcpyAsync(d_expval, b->d_expval, nc * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (d_jac && b->njac)
+        PLK_CUDA(cudaMemcpyAsync(d_jac, b->d_jac, b->njac * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    return PLK_OK;
+}
+
+static int gate_nwires(int g) { return plk_gate_num_wires(g); }
+static int gate_nparams(int g) { return plk_gate_num_params(g); }
+
+static int add_circuit(plk_batch b, int nq, const plk_op *ops, int nops, const int64_t *trainable, int ntp,
+                       int nterms, const double *coeffs, const int64_t *offsets, const int64_t *wires,
+                       const char *letters, int64_t *index) {
+    if (nq < kWinBits || nq > 30)
+        PLK_FAIL(PLK_ERR_UNSUPPORTED, "batch circuits need 4 to 30 qubits, got " + std::to_string(nq));
+    if (nops < 0 || (nops > 0 && !ops) || nterms < 0 || (nterms > 0 && (!coeffs || !offsets || !letters)))
+        PLK_FAIL(PLK_ERR_INVALID_ARG, "null argument");
+    plk_batch_s::Circ c;
+    c.nq = nq;
+    c.p0 = (int)b->params.size();
+    std::vector<double> prm;
+    auto check_w = [&](const int64_t *w, int k) -> int {
+        if (k > 0 && !w) PLK_FAIL(PLK_ERR_INVALID_ARG, "null wires");
+        for (int j = 0; j < k; j++) {
+            if (w[j] < 0 || w[j] >= nq) PLK_FAIL(PLK_ERR_INVALID_ARG, "wire out of range");
+            for (int i = 0; i < j; i++)
+                if (w[i] == w[j]) PLK_FAIL(PLK_ERR_INVALID_ARG, "repeated wire");
+        }
+        return PLK_OK;
+    };
+    // expand
+    std::vector<XOp> xs;
+    for (int i = 0; i < nops; i++) {
+        const plk_op &op = ops[i];
+        if (op.gate < 0 || op.gate >= PLK_GATE_COUNT) PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "unknown gate in op list");
+        PLK_TRY(check_w(op.wires, op.num_wires));
+        const int g = op.gate;
+        const int gw = g == PLK_GATE_MATRIX ? op.num_wires : gate_nwires(g);
+        if (gw > 0 && op.num_wires != gw)
+            PLK_FAIL(PLK_ERR_INVALID_ARG, "gate acts on " + std::to_string(gw) + " wires, got " +
+                                              std::to_string(op.num_wires));
+        const int gp = g == PLK_GATE_MATRIX ? 0 : gate_nparams(g);
+        if (op.num_params < gp || (gp > 0 && !op.params)) PLK_FAIL(PLK_ERR_INVALID_ARG, "missing gate parameters");
+        const bool inv = op.adjoint != 0;
+        auto base_op = [&](int gate, int K, const int64_t *w) {
+            XOp x;
+            x.gate = gate;
+            x.K = K;
+            for (int j = 0; j < 4; j++) x.wires[j] = j < K ? (int)w[j] : 0;
+            x.inv = inv;
+            x.pidx = -1;
+            x.slot = -1;
+            x.basis = -1;
+            x.user_matrix = -1;
+            x.kind = EK_DENSE;
+            return x;
+        };
+        if (g == PLK_GATE_IDENTITY) continue;
+        if (g == PLK_GATE_ROT || g == PLK_GATE_CROT) {
+            const int K = g == PLK_GATE_ROT ? 1 : 2;
+            const int gz = g == PLK_GATE_ROT ? PLK_GATE_RZ : PLK_GATE_CRZ;
+            const int gy = g == PLK_GATE_ROT ? PLK_GATE_RY : PLK_GATE_CRY;
+            // Rot(phi, theta, omega) = RZ(omega) RY(theta) RZ(phi); the inverse
+            // applies RZ(-omega), RY(-theta), RZ(-phi)
+            const int seq[3] = {gz, gy, gz};
+            const int pi[3] = {inv ? 2 : 0, 1, inv ? 0 : 2};
+            const int pbase = (int)prm.size();
+            for (int k = 0; k < 3; k++) prm.push_back(op.params[k]);
+            for (int k = 0; k < 3; k++) {
+                XOp x = base_op(seq[k], K, op.wires);
+                x.pidx = pbase + pi[k];
+                x.kind = is_diag_gate(seq[k]) ? EK_DIAG : EK_DENSE;
+                xs.push_back(x);
+            }
+            continue;
+        }
+        if (g == PLK_GATE_MULTIRZ) {
+            if (op.num_wires < 1) PLK_FAIL(PLK_ERR_INVALID_ARG, "MultiRZ needs at least one wire");
+            XOp x = base_op(g, 0, op.wires);
+            x.mrz_wires.assign(op.wires, op.wires + op.num_wires);
+            x.K = 1;
+            x.kind = EK_PARITY;
+            x.pidx = (int)prm.size();
+            prm.push_back(op.params[0]);
+            xs.push_back(x);
+            continue;
+        }
+        if (op.num_wires > kWinBits)
+            PLK_FAIL(PLK_ERR_UNSUPPORTED, "batch circuits support gates on at most 4 wires (and MultiRZ)");
+        XOp x = base_op(g, op.num_wires, op.wires);
+        if (g == PLK_GATE_MATRIX) {
+            if (!op.matrix) PLK_FAIL(PLK_ERR_INVALID_ARG, "matrix op without a matrix");
+            const int D = 1 << op.num_wires;
+            std::vector<double2> A(5 * (size_t)D * D, mk<double2>(0, 0));
+            for (int e = 0; e < D * D; e++) {
+                const int r = e / D, cc = e % D;
+                // adjoint: conjugate transpose
+                const int src = inv ? cc * D + r : e;
+                A[e] = mk<double2>(op.matrix[2 * src], inv ? -op.matrix[2 * src + 1] : op.matrix[2 * src + 1]);
+            }
+            x.user_matrix = (int)b->user_mats.size();
+            b->user_mats.push_back(A);
+            x.basis = (int)b->basis.size();
+            b->basis.insert(b->basis.end(), A.begin(), A.end());
+            xs.push_back(x);
+            continue;
+        }
+        if (gp == 1) {
+            x.pidx = (int)prm.size();
+            prm.push_back(op.params[0]);
+        }
+        if (g == PLK_GATE_CNOT) x.kind = EK_CX;
+        else if (is_diag_gate(g)) x.kind = EK_DIAG;
+        xs.push_back(x);
+    }
+    c.np = (int)prm.size();
+    // trainable parameters (flat indices of this circuit; all when null)
+    std::vector<int64_t> tp;
+    if (trainable) {
+        for (int t = 0; t < ntp; t++) {
+            if (trainable[t] < 0 || trainable[t] >= c.np) PLK_FAIL(PLK_ERR_INVALID_ARG, "trainable index out of range");
+            if (t > 0 && trainable[t] <= trainable[t - 1])
+                PLK_FAIL(PLK_ERR_INVALID_ARG, "trainable parameters must be sorted and unique");
+            tp.push_back(trainable[t]);
+        }
+    } else {
+        for (int t = 0; t < c.np; t++) tp.push_back(t);
+    }
+    std::vector<int> slot_of(c.np, -1);
+    for (size_t t = 0; t < tp.size(); t++) slot_of[tp[t]] = (int)t;
+    for (auto &x : xs) {
+        if (x.pidx >= 0) {
+            x.slot = slot_of[x.pidx];
+            if (x.slot >= 0 && x.gate == PLK_GATE_MATRIX)
+                PLK_FAIL(PLK_ERR_INVALID_ARG, "matrix ops have no parameter to differentiate");
+            x.pidx += c.p0;
+        }
+        if (x.basis < 0) PLK_TRY(basis_for(b, x.gate, x.inv, x.K, x.basis));
+    }
+    c.ops = std::move(xs);
+    c.ntp = (int)tp.size();
+    c.jac0 = b->njac;
+    // observable
+    for (int t = 0; t < nterms; t++) {
+        ETerm e;
+        e.x = e.z = 0;
+        e.ny = 0;
+        e.c = coeffs[t];
+        df_split_host(coeffs[t], e.ch, e.cl);
+        const int64_t o0 = offsets[t], o1 = offsets[t + 1];
+        if (o1 < o0) PLK_FAIL(PLK_ERR_INVALID_ARG, "Pauli word offsets must not decrease");
+        for (int64_t k = o0; k < o1; k++) {
+            const int64_t w = wires[k];
+            if (w < 0 || w >= nq) PLK_FAIL(PLK_ERR_INVALID_ARG, "Pauli word wire out of range");
+            const uint32_t bit = 1u << (nq - 1 - w);
+            if ((e.x | e.z) & bit) PLK_FAIL(PLK_ERR_INVALID_ARG, "repeated wire in a Pauli word");
+            switch (letters[k]) {
+            case 'X': e.x |= bit; break;
+            case 'Y': e.x |= bit; e.z |= bit; e.ny++; break;
+            case 'Z': e.z |= bit; break;
+            case 'I': break;
+            default: PLK_FAIL(PLK_ERR_INVALID_ARG, std::string("unknown Pauli letter ") + letters[k]);
+            }
+        }
+        c.terms.push_back(e);
+    }
+    b->params.insert(b->params.end(), prm.begin(), prm.end());
+    b->njac += c.ntp;
+    if (index) *index = (int64_t)b->circs.size();
+    b->circs.push_back(std::move(c));
+    b->compiled = false;
+    free_device(b);
+    return PLK_OK;
+}
+
+} // namespace plk
+
+using namespace plk;
+
+extern "C" {
+
+PLK_API int plk_gate_matrix(int32_t gate, const double *params, int32_t num_params, int32_t adjoint, int32_t num_wires,
+                            double *out) {
+    if (!out) PLK_FAIL(PLK_ERR_INVALID_ARG, "null output");
+    if (gate == PLK_GATE_MATRIX) PLK_FAIL(PLK_ERR_INVALID_ARG, "Matrix has no named gate matrix");
+    if (num_wires < 1 || num_wires > 12) PLK_FAIL(PLK_ERR_INVALID_ARG, "num_wires must be 1..12");
+    GatePlan p;
+    const double zero[3] = {0, 0, 0};
+    PLK_TRY(plan_gate(gate, num_wires, adjoint != 0, params ? params : zero, params ? num_params : 3, p));
+    std::vector<double2> M;
+    plan_dense(p, num_wires, M);
+    for (size_t i = 0; i < M.size(); i++) {
+        out[2 * i] = M[i].x;
+        out[2 * i + 1] = M[i].y;
+    }
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_create(int32_t dtype, int32_t device, plk_batch *out) {
+    if (!out) PLK_FAIL(PLK_ERR_INVALID_ARG, "null output");
+    *out = nullptr;
+    if (dtype != PLK_C64 && dtype != PLK_C128) PLK_FAIL(PLK_ERR_INVALID_ARG, "dtype must be PLK_C64 or PLK_C128");
+    DeviceCtx *d = nullptr;
+    PLK_TRY(device_ctx(device, &d));
+    PLK_CUDA(cudaSetDevice(device));
+    plk_batch b = new plk_batch_s();
+    b->dtype = dtype;
+    b->device = device;
+    b->cfg.smem_bits = dtype == PLK_C64 ? 13 : 12;
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete b;
+        cudaGetLastError();
+        PLK_FAIL(PLK_ERR_CUDA, "cannot create a stream");
+    }
+    *out = b;
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_destroy(plk_batch b) {
+    if (!b) return PLK_OK;
+    cudaSetDevice(b->device);
+    free_device(b);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_add(plk_batch b, int32_t num_qubits, const plk_op *ops, int32_t num_ops,
+                          const int64_t *trainable, int32_t num_trainable, int32_t num_terms, const double *coeffs,
+                          const int64_t *offsets, const int64_t *wires, const char *letters, int64_t *index) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    return add_circuit(b, num_qubits, ops, num_ops, trainable, num_trainable, num_terms, coeffs, offsets, wires,
+                       letters, index);
+}
+
+PLK_API int plk_batch_info(plk_batch b, int64_t *num_circuits, int64_t *num_params, int64_t *num_jac) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (num_circuits) *num_circuits = (int64_t)b->circs.size();
+    if (num_params) *num_params = (int64_t)b->params.size();
+    if (num_jac) *num_jac = b->njac;
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_circuit_info(plk_batch b, int64_t circuit, int64_t *param_offset, int32_t *num_params,
+                                   int64_t *jac_offset, int32_t *num_trainable) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (circuit < 0 || circuit >= (int64_t)b->circs.size()) PLK_FAIL(PLK_ERR_INVALID_ARG, "circuit index out of range");
+    const auto &c = b->circs[circuit];
+    if (param_offset) *param_offset = c.p0;
+    if (num_params) *num_params = c.np;
+    if (jac_offset) *jac_offset = c.jac0;
+    if (num_trainable) *num_trainable = c.ntp;
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_set_params(plk_batch b, const double *params, int64_t count) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (count != (int64_t)b->params.size())
+        PLK_FAIL(PLK_ERR_INVALID_ARG, "expected " + std::to_string(b->params.size()) + " parameters");
+    if (count && !params) PLK_FAIL(PLK_ERR_INVALID_ARG, "null parameters");
+    std::copy(params, params + count, b->params.begin());
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_set_config(plk_batch b, int32_t cluster, int32_t threads, int32_t smem_qubits,
+                                 int32_t cluster_min_qubits) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8)
+        PLK_FAIL(PLK_ERR_INVALID_ARG, "cluster must be 1, 2, 4 or 8");
+    if (threads != 256 && (threads != 512 || !kBuild512)) PLK_FAIL(PLK_ERR_INVALID_ARG, "threads must be 256");
+    const int maxsb = b->dtype == PLK_C64 ? 13 : 12;
+    if (smem_qubits < kWinBits || smem_qubits > maxsb)
+        PLK_FAIL(PLK_ERR_INVALID_ARG, "smem_qubits must be 4.." + std::to_string(maxsb));
+    if (b->dtype == PLK_C128 && threads != 256) PLK_FAIL(PLK_ERR_INVALID_ARG, "complex128 batches use 256 threads");
+    b->cfg.cluster = cluster;
+    b->cfg.threads = threads;
+    b->cfg.smem_bits = smem_qubits;
+    b->cfg.cluster_min_qubits = cluster_min_qubits;
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_get_config(plk_batch b, int32_t *cluster, int32_t *threads, int32_t *smem_qubits,
+                                 int32_t *cluster_min_qubits) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (cluster) *cluster = b->cfg.cluster;
+    if (threads) *threads = b->cfg.threads;
+    if (smem_qubits) *smem_qubits = b->cfg.smem_bits;
+    if (cluster_min_qubits) *cluster_min_qubits = b->cfg.cluster_min_qubits;
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_set_graph(plk_batch b, int32_t use_graph) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    b->use_graph = use_graph != 0;
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_run(plk_batch b, double *expvals, double *jac) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (b->circs.empty()) PLK_FAIL(PLK_ERR_INVALID_ARG, "empty batch");
+    PLK_CUDA(cudaSetDevice(b->device));
+    if (b->dtype == PLK_C128 && b->cfg.threads != 256) b->cfg.threads = 256;
+    return b->dtype == PLK_C64 ? run_host<float>(b, expvals, jac) : run_host<double>(b, expvals, jac);
+}
+
+PLK_API int plk_batch_run_device(plk_batch b, const double *d_params, double *d_expvals, double *d_jac, void *stream) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (b->circs.empty()) PLK_FAIL(PLK_ERR_INVALID_ARG, "empty batch");
+    PLK_CUDA(cudaSetDevice(b->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+    if (b->dtype == PLK_C128 && b->cfg.threads != 256) b->cfg.threads = 256;
+    return b->dtype == PLK_C64 ? run_device<float>(b, d_params, d_expvals, d_jac, st)
+                               : run_device<double>(b, d_params, d_expvals, d_jac, st);
+}
+
+PLK_API int plk_batch_last_time(plk_batch b, double *ms, int64_t *launches) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (ms) *ms = b->last_ms;
+    if (launches) *launches = b->last_launches;
+    return PLK_OK;
+}
+
+// Autotuner: times every configuration of a small grid on this batch and
+// keeps the fastest (median of `reps` graph replays after one warm-up).
+PLK_API int plk_batch_tune(plk_batch b, int32_t reps, char *report, int32_t report_len) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (b->circs.empty()) PLK_FAIL(PLK_ERR_INVALID_ARG, "empty batch");
+    PLK_CUDA(cudaSetDevice(b->device));
+    reps = std::max(1, reps);
+    const BatchConfig saved = b->cfg;
+    std::vector<BatchConfig> cands;
+    const int maxsb = b->dtype == PLK_C64 ? 13 : 12;
+    int max_nq = 0;
+    for (auto &c : b->circs) max_nq = std::max(max_nq, c.nq);
+    for (int threads : {256, 512}) {
+        if ((b->dtype == PLK_C128 || !kBuild512) && threads != 256) continue;
+        for (int cl : {1, 2, 4, 8}) {
+            for (int cmin : {maxsb + 1, maxsb + 3, maxsb + 5}) {
+                if (cl == 1 && cmin != maxsb + 1) continue;
+                if (cl > 1 && cmin > max_nq) continue;
+                BatchConfig c;
+                c.threads = threads;
+                c.cluster = cl;
+                c.smem_bits = maxsb;
+                c.cluster_min_qubits = cmin;
+                cands.push_back(c);
+            }
+        }
+    }
+    std::string rep;
+    double best = 1e300;
+    BatchConfig best_cfg = saved;
+    for (const auto &c : cands) {
+        b->cfg = c;
+        int st = plk_batch_run(b, nullptr, nullptr); // warm-up (and graph capture)
+        if (st != PLK_OK) {
+            rep += "cluster=" + std::to_string(c.cluster) + " threads=" + std::to_string(c.threads) +
+                   " cluster_min=" + std::to_string(c.cluster_min_qubits) + " failed: " + last_error() + "\n";
+            continue;
+        }
+        std::vector<double> t;
+        for (int r = 0; r < reps; r++) {
+            PLK_TRY(plk_batch_run(b, nullptr, nullptr));
+            t.push_back(b->last_ms);
+        }
+        std::sort(t.begin(), t.end());
+        const double med = t[t.size() / 2];
+        char line[160];
+        std::snprintf(line, sizeof(line), "cluster=%d threads=%d smem_qubits=%d cluster_min=%d: %.3f ms\n", c.cluster,
+                      c.threads, c.smem_bits, c.cluster_min_qubits, med);
+        rep += line;
+        if (med < best) {
+            best = med;
+            best_cfg = c;
+        }
+    }
+    b->cfg = best_cfg;
+    b->tuned = true;
+    if (report && report_len > 0) {
+        std::strncpy(report, rep.c_str(), (size_t)report_len - 1);
+        report[report_len - 1] = 0;
+    }
+    return PLK_OK;
+}
+
+} // extern "C"

@@ -57,7 +57,7 @@ template <int OP> __host__ __device__ constexpr bool pair_has_df() {
 }
 
 template <int OP, class V, class T>
-__device__ __forceinline__ void pair_op(V &x, V &y, const T *__restrict__ c) {
+__host__ __device__ __forceinline__ void pair_op(V &x, V &y, const T *__restrict__ c) {
     if constexpr (OP == P_SWAP) {
         V t = x;
         x = y;
@@ -113,7 +113,7 @@ __device__ __forceinline__ void pair_op(V &x, V &y, const T *__restrict__ c) {
 }
 
 template <int OP, class V, class T>
-__device__ __forceinline__ void quad_op(V (&v)[4], const T *__restrict__ c) {
+__host__ __device__ __forceinline__ void quad_op(V (&v)[4], const T *__restrict__ c) {
     // v[0] = |00>, v[1] = |01> (target wire set), v[2] = |10> (control), v[3] = |11>
     if constexpr (OP == Q_IXX) {
         // isingXXFunctor

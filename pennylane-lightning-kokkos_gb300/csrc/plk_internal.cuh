@@ -124,15 +124,15 @@ template <class V> __host__ __device__ __forceinline__ V mk(decltype(V::x) re, d
     r.y = im;
     return r;
 }
-template <class V> __device__ __forceinline__ V cmul(V a, V b) {
+template <class V> __host__ __device__ __forceinline__ V cmul(V a, V b) {
     return mk<V>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-template <class V> __device__ __forceinline__ V cadd(V a, V b) { return mk<V>(a.x + b.x, a.y + b.y); }
-template <class V> __device__ __forceinline__ V csub(V a, V b) { return mk<V>(a.x - b.x, a.y - b.y); }
-template <class V, class T> __device__ __forceinline__ V rmul(T s, V a) { return mk<V>(s * a.x, s * a.y); }
-template <class V> __device__ __forceinline__ V cneg(V a) { return mk<V>(-a.x, -a.y); }
-template <class V> __device__ __forceinline__ V mul_i(V a) { return mk<V>(-a.y, a.x); }   // i*a
-template <class V> __device__ __forceinline__ V mul_mi(V a) { return mk<V>(a.y, -a.x); }  // -i*a
+template <class V> __host__ __device__ __forceinline__ V cadd(V a, V b) { return mk<V>(a.x + b.x, a.y + b.y); }
+template <class V> __host__ __device__ __forceinline__ V csub(V a, V b) { return mk<V>(a.x - b.x, a.y - b.y); }
+template <class V, class T> __host__ __device__ __forceinline__ V rmul(T s, V a) { return mk<V>(s * a.x, s * a.y); }
+template <class V> __host__ __device__ __forceinline__ V cneg(V a) { return mk<V>(-a.x, -a.y); }
+template <class V> __host__ __device__ __forceinline__ V mul_i(V a) { return mk<V>(-a.y, a.x); }   // i*a
+template <class V> __host__ __device__ __forceinline__ V mul_mi(V a) { return mk<V>(a.y, -a.x); }  // -i*a
 
 // ----------------------------------------------------------------------------
 // group index maps

@@ -99,6 +99,21 @@ _SIGS = {
     "plk_adjoint_jacobian_inplace": ([_vp, C.POINTER(_vp), C.c_int32, C.POINTER(PlkOp), C.c_int32, _i64p, C.c_int32,
                                       _dp], C.c_int),
     "plk_expval_pauliz_noalloc": ([_vp, C.c_int32, C.c_int32, C.c_int32, _i64p, _dp, _vp], C.c_int),
+    "plk_gate_matrix": ([C.c_int32, _dp, C.c_int32, C.c_int32, C.c_int32, _dp], C.c_int),
+    "plk_batch_create": ([C.c_int32, C.c_int32, C.POINTER(_vp)], C.c_int),
+    "plk_batch_destroy": ([_vp], C.c_int),
+    "plk_batch_add": ([_vp, C.c_int32, C.POINTER(PlkOp), C.c_int32, _i64p, C.c_int32, C.c_int32, _dp, _i64p, _i64p,
+                       C.c_char_p, _i64p], C.c_int),
+    "plk_batch_info": ([_vp, _i64p, _i64p, _i64p], C.c_int),
+    "plk_batch_circuit_info": ([_vp, C.c_int64, _i64p, _i32p, _i64p, _i32p], C.c_int),
+    "plk_batch_set_params": ([_vp, _dp, C.c_int64], C.c_int),
+    "plk_batch_run": ([_vp, _dp, _dp], C.c_int),
+    "plk_batch_run_device": ([_vp, _dp, _dp, _dp, _vp], C.c_int),
+    "plk_batch_last_time": ([_vp, _dp, _i64p], C.c_int),
+    "plk_batch_set_config": ([_vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+    "plk_batch_get_config": ([_vp, _i32p, _i32p, _i32p, _i32p], C.c_int),
+    "plk_batch_set_graph": ([_vp, C.c_int32], C.c_int),
+    "plk_batch_tune": ([_vp, C.c_int32, C.c_char_p, C.c_int32], C.c_int),
 }
 for _name, (_args, _res) in _SIGS.items():
     _f = getattr(lib, _name)
@@ -119,6 +134,18 @@ def device_count() -> int:
     n = C.c_int(0)
     check(lib.plk_device_count(C.byref(n)))
     return n.value
+
+
+def gate_matrix(name: str, params=(), num_wires: int | None = None, adjoint: bool = False):
+    """Dense matrix (numpy complex128, wires[0] = most significant bit) of a named gate."""
+    import numpy as np
+
+    g = GATE_ID[name]
+    nw = num_wires if num_wires is not None else lib.plk_gate_num_wires(g)
+    prm = np.ascontiguousarray(np.asarray(list(params) + [0.0] * 3, dtype=np.float64))
+    out = np.zeros(2 * (1 << (2 * nw)), dtype=np.float64)
+    check(lib.plk_gate_matrix(g, prm.ctypes.data_as(_dp), len(prm), int(adjoint), nw, out.ctypes.data_as(_dp)))
+    return out.view(np.complex128).reshape(1 << nw, 1 << nw)
 
 
 def device_info(device: int = 0) -> dict:

@@ -94,3 +94,22 @@ def random_pauli_words(nq: int, count: int, seed: int, max_weight: int = 4):
         letters = "".join(str(x) for x in rng.choice(["X", "Y", "Z"], wt))
         words.append((float(rng.standard_normal()), wires, letters))
     return words
+
+
+def batch_workload(num_circuits: int = 4096, seed: int = 5, min_qubits: int = 8, max_qubits: int = 20,
+                   min_layers: int = 5, max_layers: int = 30, terms: int = 10):
+    """Independent circuits of uneven size: qubits uniform in [min_qubits,
+    max_qubits], depth uniform in [min_layers, max_layers] layers of RX, RY,
+    RZ on every wire plus a CNOT ladder, angles uniform in [0, 2*pi), and a
+    `terms`-word random Pauli Hamiltonian per circuit.
+    Returns [(num_qubits, ops, words)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(num_circuits):
+        nq = int(rng.integers(min_qubits, max_qubits + 1))
+        layers = int(rng.integers(min_layers, max_layers + 1))
+        sub = int(rng.integers(0, 2**31 - 1))
+        ops = hardware_efficient_ansatz(nq, layers, sub, rotations=("RX", "RY", "RZ"), entangler="ladder")
+        words = random_pauli_words(nq, terms, sub + 1)
+        out.append((nq, ops, words))
+    return out

@@ -121,3 +121,42 @@ def test_no_device_fails_loudly():
         m.LightningKokkos_C128(3)
     h = C.c_void_p()
     assert N.lib.plk_state_create(3, 1, 0, C.byref(h)) == 6  # PLK_ERR_NO_DEVICE
+
+
+def test_gate_matrices_match_oracle():
+    """plk_gate_matrix (host side of the gate plans, used by the batch engine)
+    equals the oracle's gate applied to every basis state."""
+    import numpy as np
+
+    import oracle as O
+    from pennylane_lightning_kokkos import _native as N
+
+    rng = np.random.default_rng(11)
+    for name in N.GATES:
+        if name in ("Matrix",):
+            continue
+        g = N.GATE_ID[name]
+        nw = N.lib.plk_gate_num_wires(g)
+        for k in ([1, 2, 3] if nw < 0 else [nw]):
+            npar = N.lib.plk_gate_num_params(g)
+            prm = [float(x) for x in rng.uniform(-np.pi, np.pi, npar)]
+            for inv in (False, True):
+                M = N.gate_matrix(name, prm, num_wires=k, adjoint=inv)
+                ref = np.zeros_like(M)
+                for c in range(1 << k):
+                    e = O.zero_state(k)
+                    e[0] = 0
+                    e[c] = 1
+                    O.apply(e, name, list(range(k)), inv, prm)
+                    ref[:, c] = e
+                np.testing.assert_allclose(M, ref, atol=1e-15, err_msg=f"{name} k={k} inv={inv}")
+
+
+def test_batch_needs_a_device():
+    import ctypes as C
+
+    from pennylane_lightning_kokkos import _native as N
+
+    h = C.c_void_p()
+    assert N.lib.plk_batch_create(0, 0, C.byref(h)) == 6  # PLK_ERR_NO_DEVICE
+    assert "no CUDA device" in N.last_error()
