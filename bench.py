@@ -26,6 +26,15 @@ Printed JSON line:
                + CNOT ladder, 100-term Pauli Hamiltonian) in complex64 with
                FP64 accumulation vs complex128, seconds per gradient and the
                largest gradient difference
+  batch      - 4096 circuits (8-20 qubits, 5-30 layers, 10-term Hamiltonians),
+               forward + <H> + adjoint gradient in one persistent complex64
+               launch replayed as a CUDA graph (autotuned), circuits/s,
+               against a per-circuit loop of the plain path and the oracle
+  plain_20q  - 20-qubit complex128 circuit (600 parameters), 20 <PauliZ> and
+               the 20 x 600 Jacobian through the reference-facing module,
+               against the oracle on the host cores
+  precision  - (--precision) 32-qubit complex64 vs 31-qubit complex128 at
+               equal bytes, 200-word Hamiltonian, error against complex128
 `--impl reference` times the oracle (the CPU restatement of the reference
 functors) on the host cores instead.  For --gpus N
 under torchrun every rank runs an independent replica (weak scaling).
@@ -65,6 +74,11 @@ def parse_args(argv=None):
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--adjoint-nq", type=int, default=26)
     ap.add_argument("--adjoint-layers", type=int, default=40)
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-circuits", type=int, default=4096)
+    ap.add_argument("--no-plain20", action="store_true")
+    ap.add_argument("--precision", action="store_true",
+                    help="also run the equal-bytes precision config (32-qubit complex64 vs 31-qubit complex128)")
     return ap.parse_args(argv)
 
 
@@ -412,6 +426,276 @@ def run_adjoint(args, device, torch):
     return out
 
 
+# ---------------------------------------------------------- batching C5 --
+def _words_obs(m, bits, words):
+    letters = {"X": "PauliX", "Y": "PauliY", "Z": "PauliZ"}
+    L = lambda name: getattr(m, name + "_C" + bits)  # noqa: E731
+    dt = np.float64 if bits == "128" else np.float32
+    terms = []
+    for c, w, l in words:
+        fac = [L("NamedObsKokkos")(letters[x], [wi]) for wi, x in zip(w, l)]
+        terms.append(fac[0] if len(fac) == 1 else L("TensorProdObsKokkos")(fac))
+    return L("HamiltonianKokkos")(np.array([c for c, _, _ in words], dtype=dt), terms)
+
+
+def plain_circuit_gradient(m, bits, device, nq, ops, words):
+    """One circuit through the reference-facing module: state, tape, <H>,
+    adjoint Jacobian of every parameter (what the reference device does per tape)."""
+    L = lambda name: getattr(m, name + "_C" + bits)  # noqa: E731
+    dt = np.float64 if bits == "128" else np.float32
+    cdt = np.complex128 if bits == "128" else np.complex64
+    sv = L("LightningKokkos")(nq, m.InitializationSettings().set_device_id(device))
+    names, wires, invs, prms = [o[0] for o in ops], [o[1] for o in ops], [o[2] for o in ops], [o[3] for o in ops]
+    sv.apply(names, wires, invs, prms)
+    ev = sv.ExpectationValuePauliSum([c for c, _, _ in words], [w for _, w, _ in words], [l for _, _, l in words])
+    adj = L("AdjointJacobianKokkos")()
+    tape = adj.create_ops_list(names, [np.array(p, dtype=dt) for p in prms], wires, invs,
+                               [np.array([], dtype=cdt)] * len(ops))
+    npar = sum(1 for p in prms if p)
+    jac = np.asarray(adj.adjoint_jacobian(sv, [_words_obs(m, bits, words)], tape, list(range(npar))))[0]
+    return ev, jac
+
+
+def run_batch(args, device, torch):
+    """Batching: forward + <H> + adjoint gradient of every circuit of a
+    seeded uneven batch in one persistent complex64 launch (CUDA graph),
+    against a per-circuit loop of the plain path and the oracle."""
+    import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
+    from pennylane_lightning_kokkos.batch import CircuitBatch
+    from pennylane_lightning_kokkos.circuits import batch_workload_packed, packed_to_ops
+
+    n = args.batch_circuits
+    wl = batch_workload_packed(n, seed=5)
+    work = np.array([len(pk["gates"]) * float(1 << nq) for nq, pk, _ in wl])
+    gate_apps = sum(len(pk["gates"]) for _, pk, _ in wl)
+    # autotune on a one-in-sixteen subsample, then run the whole batch with the winner
+    sub = CircuitBatch("c64", device)
+    for nq, pk, words in wl[::16]:
+        sub.add_packed(nq, pk, words)
+    t = time.perf_counter()
+    report = sub.tune(reps=1)
+    tune_s = time.perf_counter() - t
+    cfg = sub.get_config()
+    sub.close()
+    b = CircuitBatch("c64", device)
+    for nq, pk, words in wl:
+        b.add_packed(nq, pk, words)
+    b.set_config(cluster=cfg["cluster"], smem_qubits=cfg["smem_qubits"], cluster_min_qubits=cfg["cluster_min_qubits"],
+                 ctas_per_sm=cfg["ctas_per_sm"])
+    t = time.perf_counter()
+    b.run()
+    first_s = time.perf_counter() - t
+    _, npar, njac = b.info()
+    params = np.concatenate([pk["params"] for _, pk, _ in wl])
+    b.run(params)
+    dev_ms, wall_s = [], []
+    for _ in range(3):
+        t = time.perf_counter()
+        ev, jac = b.run(params)
+        wall_s.append(time.perf_counter() - t)
+        dev_ms.append(b.last_time()[0])
+    launches = b.last_time()[1]
+    grads = b.gradients(jac)
+    b.close()
+    ms = statistics.median(dev_ms)
+    out = {"circuits": n, "qubits": "uniform 8-20", "layers": "uniform 5-30 (RX, RY, RZ + CNOT ladder)",
+           "hamiltonian_terms": 10, "dtype": "complex64 state, double-float accumulation",
+           "params": int(npar), "gate_applications_forward": int(gate_apps),
+           "tuned_config": cfg, "tune_seconds": tune_s, "first_run_seconds": first_s,
+           "device_ms": ms, "circuits_per_s": n / (ms / 1e3),
+           "e2e_circuits_per_s": n / statistics.median(wall_s),
+           "e2e_api": "CircuitBatch.run (parameters in, <H> and gradients out, host arrays)",
+           "gate_applications_per_s": gate_apps / (ms / 1e3), "kernel_launches_per_run": int(launches),
+           "tune_report": report.strip().splitlines()}
+    # accuracy: complex128 batch on a sample
+    idx = list(range(0, n, max(1, n // 64)))
+    b128 = CircuitBatch("c128", device)
+    for i in idx:
+        b128.add_packed(wl[i][0], wl[i][1], wl[i][2])
+    ev128, jac128 = b128.run()
+    g128 = b128.gradients(jac128)
+    b128.close()
+    out["max_abs_expval_diff_c64_vs_c128"] = float(max(abs(ev[i] - ev128[k]) for k, i in enumerate(idx)))
+    out["max_abs_grad_diff_c64_vs_c128"] = float(max(np.max(np.abs(grads[i] - g128[k])) for k, i in enumerate(idx)))
+    out["accuracy_sample"] = f"{len(idx)} circuits (every {max(1, n // 64)}th), complex128 batch as reference"
+    # per-circuit loop of the plain path (reference-facing module), on a sample
+    idx = list(range(0, n, max(1, n // 32)))
+    plain = [(wl[i][0], packed_to_ops(wl[i][1]), wl[i][2]) for i in idx]
+    plain_circuit_gradient(m, "64", device, *plain[0])
+    torch.cuda.synchronize(device)
+    t = time.perf_counter()
+    for nq, ops, words in plain:
+        plain_circuit_gradient(m, "64", device, nq, ops, words)
+    torch.cuda.synchronize(device)
+    dt = time.perf_counter() - t
+    frac = work[idx].sum() / work.sum()
+    out["plain_loop"] = {"sample": f"{len(idx)} circuits (every {max(1, n // 32)}th), LightningKokkos_C64 + "
+                                   "AdjointJacobianKokkos_C64 per circuit",
+                         "seconds": dt, "extrapolated_seconds_full_batch": dt / frac,
+                         "circuits_per_s": n / (dt / frac)}
+    out["speedup_vs_plain_loop"] = (dt / frac) / (ms / 1e3)
+    return out
+
+
+def run_batch_cpu(args):
+    """The oracle (CPU restatement, OpenMP on every host core) on a sample of
+    the batch: forward, <H>, adjoint Jacobian per circuit."""
+    import oracle as O
+    from pennylane_lightning_kokkos.circuits import batch_workload_packed, packed_to_ops
+
+    threads = os.cpu_count() or 1
+    O.set_num_threads(threads)
+    n = args.batch_circuits
+    wl = batch_workload_packed(n, seed=5)
+    work = np.array([len(pk["gates"]) * float(1 << nq) for nq, pk, _ in wl])
+    idx = list(range(0, n, max(1, n // 8)))
+    letters = {"X": "PauliX", "Y": "PauliY", "Z": "PauliZ"}
+    t = time.perf_counter()
+    for i in idx:
+        nq, pk, words = wl[i]
+        ops = packed_to_ops(pk)
+        psi = O.run_ops(O.zero_state(nq), ops)
+        obs = ("hamiltonian", [c for c, _, _ in words],
+               [("tensor", [("named", letters[x], [wi]) for wi, x in zip(w, l)]) for _, w, l in words])
+        O.expval_observable(psi, obs)
+        O.adjoint_jacobian(psi, [obs], ops, list(range(sum(1 for o in ops if o[3]))))
+    dt = time.perf_counter() - t
+    frac = work[idx].sum() / work.sum()
+    return {"circuits_per_s": n / (dt / frac), "cores": threads, "kind": "port",
+            "sample": f"{len(idx)} circuits (every {max(1, n // 8)}th), {dt:.1f} s, extrapolated by gate work"}
+
+
+# ----------------------------------------------------------- plain 20q C1 --
+def run_plain20(args, device, torch):
+    """Plain method, 20 qubits complex128: 10 layers of RX, RY, RZ on every wire
+    + CNOT ring (600 parameters, 800 ops), <PauliZ> on every wire and the
+    20 x 600 adjoint Jacobian, through the reference-facing module; the oracle
+    runs the same circuit on the host cores."""
+    import oracle as O
+    import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
+    from pennylane_lightning_kokkos.circuits import hardware_efficient_ansatz
+
+    nq = 20
+    ops = hardware_efficient_ansatz(nq, 10, seed=1, rotations=("RX", "RY", "RZ"), entangler="ring")
+    npar = sum(1 for o in ops if o[3])
+    names, wires, invs, prms = [o[0] for o in ops], [o[1] for o in ops], [o[2] for o in ops], [o[3] for o in ops]
+
+    def gpu():
+        sv = m.LightningKokkos_C128(nq, m.InitializationSettings().set_device_id(device))
+        sv.apply(names, wires, invs, prms)
+        ev = np.array([sv.ExpectationValue("PauliZ", [w], [], np.array([], np.complex128)) for w in range(nq)])
+        adj = m.AdjointJacobianKokkos_C128()
+        tape = adj.create_ops_list(names, [np.array(p, dtype=np.float64) for p in prms], wires, invs,
+                                   [np.array([], dtype=np.complex128)] * len(ops))
+        obs = [m.NamedObsKokkos_C128("PauliZ", [w]) for w in range(nq)]
+        jac = np.asarray(adj.adjoint_jacobian(sv, obs, tape, list(range(npar))))
+        return ev, jac
+
+    gpu()
+    torch.cuda.synchronize(device)
+    ts = []
+    for _ in range(3):
+        t = time.perf_counter()
+        ev, jac = gpu()
+        ts.append(time.perf_counter() - t)
+    threads = os.cpu_count() or 1
+    O.set_num_threads(threads)
+    t = time.perf_counter()
+    psi = O.run_ops(O.zero_state(nq), ops)
+    ev_o = np.array([O.expval_named(psi, "PauliZ", [w]) for w in range(nq)])
+    jac_o = O.adjoint_jacobian(psi, [("named", "PauliZ", [w]) for w in range(nq)], ops, list(range(npar)))
+    cpu_s = time.perf_counter() - t
+    return {"qubits": nq, "dtype": "complex128", "ops": len(ops), "params": npar, "observables": nq,
+            "gpu_seconds_per_circuit": statistics.median(ts),
+            "cpu_oracle_seconds_per_circuit": cpu_s, "cpu_cores": threads,
+            "speedup_vs_cpu_oracle": cpu_s / statistics.median(ts),
+            "max_abs_expval_diff_vs_oracle": float(np.max(np.abs(ev - ev_o))),
+            "max_abs_jac_diff_vs_oracle": float(np.max(np.abs(jac - jac_o))),
+            "api": "LightningKokkos_C128.apply / ExpectationValue / AdjointJacobianKokkos_C128.adjoint_jacobian"}
+
+
+# ------------------------------------------------------- precision C3 --
+def run_precision(args, device, torch):
+    """Equal bytes: 32-qubit complex64 vs 31-qubit complex128 (32 GiB each),
+    20 layers of RY, RZ + CNOT ladder, <H> of 200 Pauli words; the error of
+    complex64 is stated against complex128 at 32 qubits (64 GiB)."""
+    from pennylane_lightning_kokkos import _native as N
+    from pennylane_lightning_kokkos.circuits import hardware_efficient_ansatz, random_pauli_words
+
+    out = {}
+    words = {}
+    for nq in (31, 32):
+        words[nq] = random_pauli_words(nq, 200, seed=3)
+
+    def run(nq, dtype):
+        ops = hardware_efficient_ansatz(nq, 20, seed=3, rotations=("RY", "RZ"), entangler="ladder")
+        h = C.c_void_p()
+        N.check(N.lib.plk_state_create(nq, dtype, device, C.byref(h)))
+        arr = (N.PlkOp * len(ops))()
+        keep = []
+        for i, (name, w, inv, p) in enumerate(ops):
+            wa = np.array(w, dtype=np.int64)
+            pa = np.array(p or [0.0], dtype=np.float64)
+            keep += [wa, pa]
+            arr[i] = N.PlkOp(N.GATE_ID[name], len(w), 0, len(p), wa.ctypes.data_as(C.POINTER(C.c_int64)),
+                             pa.ctypes.data_as(C.POINTER(C.c_double)), None)
+        wd = words[nq]
+        co = np.array([c for c, _, _ in wd])
+        of = np.cumsum([0] + [len(w) for _, w, _ in wd]).astype(np.int64)
+        wi = np.array([x for _, w, _ in wd for x in w], dtype=np.int64)
+        le = "".join(l for _, _, l in wd).encode()
+        torch.cuda.synchronize(device)
+        t = time.perf_counter()
+        N.check(N.lib.plk_apply_ops(h, arr, len(ops)))
+        N.check(N.lib.plk_state_synchronize(h))
+        t_g = time.perf_counter() - t
+        v = C.c_double()
+        t = time.perf_counter()
+        N.check(N.lib.plk_expval_pauli_sum(h, len(co), co.ctypes.data_as(C.POINTER(C.c_double)),
+                                           of.ctypes.data_as(C.POINTER(C.c_int64)),
+                                           wi.ctypes.data_as(C.POINTER(C.c_int64)), le, C.byref(v)))
+        t_e = time.perf_counter() - t
+        return h, len(ops), t_g, t_e, v.value
+
+    res = {}
+    for nq, dt, name in ((32, N.PLK_C64, "c64_32q"), (31, N.PLK_C128, "c128_31q")):
+        h, nops, t_g, t_e, val = run(nq, dt)
+        ops = hardware_efficient_ansatz(nq, 20, seed=3, rotations=("RY", "RZ"), entangler="ladder")
+        touched = sum(0.5 if o[0] == "CNOT" else 1.0 for o in ops)  # CNOT moves half of the amplitudes
+        nbytes = 2 * (1 << nq) * (8 if dt == N.PLK_C64 else 16) * touched
+        res[name] = {"gates": nops, "gates_seconds": t_g, "gates_GBps_algorithmic": nbytes / t_g / 1e9,
+                     "expval_seconds": t_e, "expval": val}
+        N.lib.plk_state_destroy(h)
+    # error of complex64 at 32 qubits against complex128 at 32 qubits
+    h64, _, _, _, v64 = run(32, N.PLK_C64)
+    h128, _, _, _, v128 = run(32, N.PLK_C128)
+    p64, p128 = C.c_void_p(), C.c_void_p()
+    nq_, dt_ = C.c_int(), C.c_int()
+    N.check(N.lib.plk_state_get(h64, C.byref(nq_), C.byref(dt_), C.byref(p64)))
+    N.check(N.lib.plk_state_get(h128, C.byref(nq_), C.byref(dt_), C.byref(p128)))
+    n = 1 << 32
+    chunk = 1 << 28
+    maxd = 0.0
+
+    class _Arr:
+        def __init__(self, ptr, shape, typestr):
+            self.__cuda_array_interface__ = {"data": (ptr, False), "shape": shape, "typestr": typestr, "version": 3}
+
+    for off in range(0, n, chunk):
+        a = torch.as_tensor(_Arr(p64.value + off * 8, (chunk,), "<c8"), device=f"cuda:{device}")
+        b = torch.as_tensor(_Arr(p128.value + off * 16, (chunk,), "<c16"), device=f"cuda:{device}")
+        maxd = max(maxd, float((a.to(torch.complex128) - b).abs().max()))
+    N.lib.plk_state_destroy(h64)
+    N.lib.plk_state_destroy(h128)
+    res["error_c64_vs_c128_32q"] = {"expval_abs": abs(v64 - v128), "state_max_abs": maxd,
+                                     "expval_c128": v128,
+                                     "reference": "complex128 GPU path at 32 qubits (parity-checked against the "
+                                                  "FP64 oracle at <= 26 qubits)"}
+    res["equal_bytes_speed_ratio_gates"] = res["c128_31q"]["gates_seconds"] / res["c64_32q"]["gates_seconds"]
+    out.update(res)
+    return out
+
+
 # ------------------------------------------------------------------ main --
 def main(argv=None):
     args = parse_args(argv)
@@ -491,8 +775,30 @@ def main(argv=None):
             result["adjoint_26q"] = run_adjoint(args, device, torch)
         except Exception as e:  # report, do not hide the main number
             result["adjoint_26q"] = {"error": repr(e)}
+    if rank == 0 and not args.no_batch:
+        try:
+            result["batch"] = run_batch(args, device, torch)
+        except Exception as e:
+            result["batch"] = {"error": repr(e)}
+    if rank == 0 and not args.no_plain20:
+        try:
+            result["plain_20q"] = run_plain20(args, device, torch)
+        except Exception as e:
+            result["plain_20q"] = {"error": repr(e)}
+    if rank == 0 and args.precision:
+        try:
+            result["precision"] = run_precision(args, device, torch)
+        except Exception as e:
+            result["precision"] = {"error": repr(e)}
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = run_cpu_baseline(args)
+        if not args.no_batch and "error" not in result.get("batch", {}):
+            try:
+                result["batch"]["cpu_oracle"] = run_batch_cpu(args)
+                result["batch"]["speedup_vs_cpu_oracle"] = (result["batch"]["circuits_per_s"]
+                                                            / result["batch"]["cpu_oracle"]["circuits_per_s"])
+            except Exception as e:
+                result["batch"]["cpu_oracle"] = {"error": repr(e)}
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()

@@ -289,13 +289,17 @@ PLK_API int plk_batch_run_device(plk_batch b, const double *d_params, double *d_
                                  void *cuda_stream);
 /* device time (CUDA events) and kernel launches of the last plk_batch_run */
 PLK_API int plk_batch_last_time(plk_batch b, double *ms, int64_t *launches);
-/* launch configuration: CTAs per cluster (1, 2, 4, 8), threads per CTA (256,
- * 512), circuits of at most smem_qubits qubits run in shared memory, circuits
- * of at least cluster_min_qubits qubits are shared by a cluster */
+/* launch configuration: CTAs per cluster (1, 2, 4, 8), threads per CTA (256),
+ * circuits of at most smem_qubits qubits run in shared memory, circuits of at
+ * least cluster_min_qubits qubits are shared by a cluster */
 PLK_API int plk_batch_set_config(plk_batch b, int32_t cluster, int32_t threads, int32_t smem_qubits,
                                  int32_t cluster_min_qubits);
 PLK_API int plk_batch_get_config(plk_batch b, int32_t *cluster, int32_t *threads, int32_t *smem_qubits,
                                  int32_t *cluster_min_qubits);
+/* CTAs per SM: 1 (255 registers per thread; complex64 circuits of up to 13
+ * qubits in shared memory) or 2 (complex64 only; 128 registers, up to 12) */
+PLK_API int plk_batch_set_occupancy(plk_batch b, int32_t ctas_per_sm);
+PLK_API int plk_batch_get_occupancy(plk_batch b, int32_t *ctas_per_sm);
 PLK_API int plk_batch_set_graph(plk_batch b, int32_t use_graph);
 /* autotuner: times a grid of configurations on this batch (median of reps
  * runs each) and keeps the fastest; a text report goes to `report` */

@@ -219,6 +219,7 @@ struct XOp { // an op after expansion (Rot -> RZ RY RZ)
 struct BatchConfig {
     int cluster = 8;        // CTAs per cluster for the largest circuits
     int threads = 256;      // threads per CTA
+    int ctas_per_sm = 1;    // 1 or 2 (complex64): register budget 255 or 128 per thread
     int smem_bits = 13;     // circuits with at most this many qubits stay in shared memory
     int cluster_min_qubits = 17; // circuits with at least this many qubits go to clusters
 };
@@ -657,8 +658,8 @@ __device__ __forceinline__ void esync(int C) {
 }
 
 template <class T, bool BWD>
-__device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps], c2_t<T> (&hv)[kWinAmps], uint64_t base,
-                                          const uint64_t (&bb)[4], const c2_t<T> *__restrict__ mats, EAcc<T> &acc,
+__device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps], c2_t<T> (&hv)[kWinAmps], uint32_t base,
+                                          const uint32_t (&bb)[4], const c2_t<T> *__restrict__ mats, EAcc<T> &acc,
                                           EAcc<T> &acc1) {
     using V = c2_t<T>;
     const bool tr = BWD && op.red != 0xff;
@@ -738,7 +739,7 @@ __device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps]
         T t = 0;
 #pragma unroll
         for (int j = 0; j < kWinAmps; j++) {
-            const uint64_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
                                  ((j & 8) ? bb[3] : 0);
             const bool one = (idx >> b0) & 1u;
             if (tr) {
@@ -759,9 +760,9 @@ __device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps]
         const bool parity = op.kind == EK_PARITY;
 #pragma unroll
         for (int j = 0; j < kWinAmps; j++) {
-            const uint64_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
                                  ((j & 8) ? bb[3] : 0);
-            const uint32_t g = parity ? (uint32_t)(__popcll(idx & (uint64_t)op.bits) & 1) : diag_index(idx, op.bits, op.K);
+            const uint32_t g = parity ? (uint32_t)(__popc(idx & op.bits) & 1) : diag_index(idx, op.bits, op.K);
             const V e = mats[op.mat + g];
             if (tr) {
                 // generator diagonal: MultiRZ (-1)^parity, otherwise real entries 0, +-1
@@ -775,24 +776,24 @@ __device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps]
 }
 
 template <class T, int NT, int MODE, bool BWD>
-__device__ __noinline__ void run_window(const EngArgs<T> &a, const EWin &w, int nq, c2_t<T> *lam, c2_t<T> *hl, uint64_t t0,
-                                        uint64_t tstep, typename EAcc<T>::Slot *part) {
+__device__ __noinline__ void run_window(const EngArgs<T> &a, const EWin &w, int nq, c2_t<T> *lam, c2_t<T> *hl, uint32_t t0,
+                                        uint32_t tstep, typename EAcc<T>::Slot *part) {
     using V = c2_t<T>;
     const int lane = threadIdx.x & 31;
-    const uint64_t nu = 1ull << (nq - kWinBits);
-    const uint64_t bb[4] = {1ull << w.rb[0], 1ull << w.rb[1], 1ull << w.rb[2], 1ull << w.rb[3]};
-    for (uint64_t u = t0; u - lane < nu; u += tstep) {
+    const uint32_t nu = 1u << (nq - kWinBits);
+    const uint32_t bb[4] = {1u << w.rb[0], 1u << w.rb[1], 1u << w.rb[2], 1u << w.rb[3]};
+    for (uint32_t u = t0; u - lane < nu; u += tstep) {
         const bool act = u < nu;
-        uint64_t base = u;
+        uint32_t base = u;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const uint64_t lo = base & (bb[i] - 1);
+            const uint32_t lo = base & (bb[i] - 1);
             base = ((base ^ lo) << 1) | lo;
         }
         V lv[kWinAmps], hv[kWinAmps];
 #pragma unroll
         for (int j = 0; j < kWinAmps; j++) {
-            const uint64_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
                                  ((j & 8) ? bb[3] : 0);
             lv[j] = act ? eld<T, MODE>(lam, idx) : mk<V>(0, 0);
             if (BWD) hv[j] = act ? eld<T, MODE>(hl, idx) : mk<V>(0, 0);
@@ -811,7 +812,7 @@ __device__ __noinline__ void run_window(const EngArgs<T> &a, const EWin &w, int 
         if (act) {
 #pragma unroll
             for (int j = 0; j < kWinAmps; j++) {
-                const uint64_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
                                      ((j & 8) ? bb[3] : 0);
                 est<T, MODE>(lam, idx, lv[j]);
                 if (BWD) est<T, MODE>(hl, idx, hv[j]);
@@ -850,20 +851,20 @@ __device__ void finalize_window(const EngArgs<T> &a, const ECirc &ci, const EWin
 // H lambda and <lambda|H|lambda>; H = sum_w c_w P_w with
 // <i|P|lambda> = i^ny (-1)^popc((i ^ x) & z) lambda[i ^ x]
 template <class T, int NT, int MODE>
-__device__ void h_pass(const EngArgs<T> &a, const ECirc &ci, c2_t<T> *lam, c2_t<T> *hl, uint64_t t0, uint64_t tstep,
+__device__ void h_pass(const EngArgs<T> &a, const ECirc &ci, c2_t<T> *lam, c2_t<T> *hl, uint32_t t0, uint32_t tstep,
                        double *misc, int rank, int C) {
     using V = c2_t<T>;
     constexpr int NW = NT / 32;
-    const uint64_t N = 1ull << ci.nq;
+    const uint32_t N = 1u << ci.nq;
     EAcc<T> acc;
-    for (uint64_t i = t0; i < N; i += tstep) {
+    for (uint32_t i = t0; i < N; i += tstep) {
         const V li = eld<T, MODE>(lam, i);
         V hs = mk<V>(0, 0);
         for (int k = 0; k < ci.nterms; k++) {
             const ETerm tm = a.terms[ci.term0 + k];
-            const uint64_t j = i ^ (uint64_t)tm.x;
+            const uint32_t j = i ^ tm.x;
             const V v = eld<T, MODE>(lam, j);
-            const int q = (tm.ny + 2 * (__popcll(j & (uint64_t)tm.z) & 1)) & 3;
+            const int q = (tm.ny + 2 * (__popc(j & tm.z) & 1)) & 3;
             const V u = q == 0 ? v : (q == 1 ? mul_i(v) : (q == 2 ? cneg(v) : mul_mi(v)));
             const T c = (T)tm.c;
             hs = mk<V>(hs.x + c * u.x, hs.y + c * u.y);
@@ -884,15 +885,16 @@ __device__ void h_pass(const EngArgs<T> &a, const ECirc &ci, c2_t<T> *lam, c2_t<
     }
 }
 
-template <class T, int NT, int MODE>
+template <class T, int NT, int MODE, int NBUF>
 __device__ void run_circuit(const EngArgs<T> &a, int cid, int rank, int C, c2_t<T> *lam, c2_t<T> *hl,
                             typename EAcc<T>::Slot *part, double *misc) {
     using V = c2_t<T>;
     constexpr int NW = NT / 32;
     const ECirc ci = a.circ[cid];
-    const uint64_t N = 1ull << ci.nq;
-    const uint64_t t0 = (uint64_t)rank * NT + threadIdx.x, tstep = (uint64_t)C * NT;
-    for (uint64_t i = t0; i < N; i += tstep) est<T, MODE>(lam, i, mk<V>(i == 0 ? (T)1 : (T)0, (T)0));
+    // state indices fit 32 bits (at most 30 qubits)
+    const uint32_t N = 1u << ci.nq;
+    const uint32_t t0 = (uint32_t)rank * NT + threadIdx.x, tstep = (uint32_t)C * NT;
+    for (uint32_t i = t0; i < N; i += tstep) est<T, MODE>(lam, i, mk<V>(i == 0 ? (T)1 : (T)0, (T)0));
     esync(C);
     for (int k = 0; k < ci.nfw; k++) {
         const EWin w = a.win[ci.fw0 + k];
@@ -908,10 +910,13 @@ __device__ void run_circuit(const EngArgs<T> &a, int cid, int rank, int C, c2_t<
     }
     for (int k = 0; k < ci.nbw; k++) {
         const EWin w = a.win[ci.bw0 + k];
-        typename EAcc<T>::Slot *rb = part + (k & 1) * kMaxWinTrain * NT;
+        // two partial buffers: finalizing window k overlaps window k + 1;
+        // one buffer: a barrier after finalizing
+        typename EAcc<T>::Slot *rb = part + (NBUF == 2 ? (k & 1) : 0) * kMaxWinTrain * NT;
         run_window<T, NT, MODE, true>(a, w, ci.nq, lam, hl, t0, tstep, rb);
         esync(C);
         finalize_window<T, NT>(a, ci, w, rb, rank, C);
+        if (NBUF == 1) esync(C);
     }
     esync(C);
     if (C > 1 && rank == 0) {
@@ -923,8 +928,12 @@ __device__ void run_circuit(const EngArgs<T> &a, int cid, int rank, int C, c2_t<
     }
 }
 
-template <class T, int NT>
-__global__ void __launch_bounds__(NT, 1) k_batch_engine(const EngArgs<T> a) {
+// MINB CTAs per SM: 1 (255 registers, two partial buffers, states of up to
+// 13 qubits in shared memory for complex64) or 2 (128 registers, one buffer,
+// up to 12 qubits)
+template <class T, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_batch_engine(const EngArgs<T> a) {
+    constexpr int NBUF = MINB == 1 ? 2 : 1;
     using V = c2_t<T>;
     constexpr int NW = NT / 32;
     extern __shared__ __align__(16) unsigned char esmem[];
@@ -932,9 +941,9 @@ __global__ void __launch_bounds__(NT, 1) k_batch_engine(const EngArgs<T> a) {
     V *s_hl = s_lam + (1u << a.smem_bits);
     using Slot = typename EAcc<T>::Slot;
     Slot *s_part = (Slot *)(s_hl + (1u << a.smem_bits)); // [2][kMaxWinTrain][NT]
-    double *s_misc = (double *)(s_part + 2 * kMaxWinTrain * NT);
+    double *s_misc = (double *)(s_part + NBUF * kMaxWinTrain * NT);
     __shared__ int s_cur;
-    for (int i = threadIdx.x; i < 2 * kMaxWinTrain * NT; i += NT) s_part[i] = Slot{};
+    for (int i = threadIdx.x; i < NBUF * kMaxWinTrain * NT; i += NT) s_part[i] = Slot{};
     __syncthreads();
     V *slot_cta = a.scratch ? a.scratch + (uint64_t)blockIdx.x * 2 * a.slot_amps : nullptr;
     if (a.n_cl > 0) {
@@ -948,7 +957,7 @@ __global__ void __launch_bounds__(NT, 1) k_batch_engine(const EngArgs<T> a) {
             const int c = *cl.map_shared_rank(&s_cur, 0);
             cl.sync();
             if (c >= a.n_cl) break;
-            run_circuit<T, NT, EM_GLOBAL>(a, a.order_cl[c], rank, C, slot_cl, slot_cl + a.slot_amps, s_part, s_misc);
+            run_circuit<T, NT, EM_GLOBAL, NBUF>(a, a.order_cl[c], rank, C, slot_cl, slot_cl + a.slot_amps, s_part, s_misc);
         }
     }
     for (;;) {
@@ -958,23 +967,23 @@ __global__ void __launch_bounds__(NT, 1) k_batch_engine(const EngArgs<T> a) {
         __syncthreads();
         if (c >= a.n_solo) break;
         const int cid = a.order_solo[c];
-        if (a.circ[cid].nq <= a.smem_bits) run_circuit<T, NT, EM_SMEM>(a, cid, 0, 1, s_lam, s_hl, s_part, s_misc);
-        else run_circuit<T, NT, EM_GLOBAL>(a, cid, 0, 1, slot_cta, slot_cta + a.slot_amps, s_part, s_misc);
+        if (a.circ[cid].nq <= a.smem_bits) run_circuit<T, NT, EM_SMEM, NBUF>(a, cid, 0, 1, s_lam, s_hl, s_part, s_misc);
+        else run_circuit<T, NT, EM_GLOBAL, NBUF>(a, cid, 0, 1, slot_cta, slot_cta + a.slot_amps, s_part, s_misc);
     }
 }
 
 // ------------------------------------------------------------- launching --
-template <class T, int NT> static size_t engine_smem(int smem_bits) {
-    return 2 * (sizeof(c2_t<T>) << smem_bits) + 2 * kMaxWinTrain * NT * sizeof(typename EAcc<T>::Slot) +
+template <class T, int NT, int MINB> static size_t engine_smem(int smem_bits) {
+    return 2 * (sizeof(c2_t<T>) << smem_bits) + (MINB == 1 ? 2 : 1) * kMaxWinTrain * NT * sizeof(typename EAcc<T>::Slot) +
            (NT / 32 + 8) * sizeof(double);
 }
+template <class T, int MINB> static int max_smem_bits() { return sizeof(T) == 4 ? (MINB == 1 ? 13 : 12) : 12; }
 
-template <class T, int NT> static int plan_launch(plk_batch b, LaunchPlan &lp) {
+template <class T, int NT, int MINB> static int plan_launch(plk_batch b, LaunchPlan &lp) {
     const BatchConfig &cfg = b->cfg;
-    const int maxsb = sizeof(T) == 4 ? 13 : 12;
-    const int sb = std::min(cfg.smem_bits, maxsb);
-    lp.smem = engine_smem<T, NT>(sb);
-    auto kern = k_batch_engine<T, NT>;
+    const int sb = std::min(cfg.smem_bits, max_smem_bits<T, MINB>());
+    lp.smem = engine_smem<T, NT, MINB>(sb);
+    auto kern = k_batch_engine<T, NT, MINB>;
     PLK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lp.smem));
     DeviceCtx *d = nullptr;
     PLK_TRY(device_ctx(b->device, &d));
@@ -1022,7 +1031,7 @@ template <class T, int NT> static int plan_launch(plk_batch b, LaunchPlan &lp) {
     return PLK_OK;
 }
 
-template <class T, int NT> static int launch_engine(plk_batch b, const LaunchPlan &lp, cudaStream_t st) {
+template <class T, int NT, int MINB> static int launch_engine(plk_batch b, const LaunchPlan &lp, cudaStream_t st) {
     using V = c2_t<T>;
     EngArgs<T> a;
     a.circ = (const ECirc *)b->d_circ;
@@ -1042,7 +1051,7 @@ template <class T, int NT> static int launch_engine(plk_batch b, const LaunchPla
     a.jac = b->d_jac;
     a.jac_part = b->d_jac_part;
     a.ev_part = b->d_ev_part;
-    a.smem_bits = std::min(b->cfg.smem_bits, sizeof(T) == 4 ? 13 : 12);
+    a.smem_bits = std::min(b->cfg.smem_bits, max_smem_bits<T, MINB>());
     cudaLaunchConfig_t lc = {};
     cudaLaunchAttribute at[1];
     lc.gridDim = dim3(lp.grid);
@@ -1057,18 +1066,15 @@ template <class T, int NT> static int launch_engine(plk_batch b, const LaunchPla
         lc.attrs = at;
         lc.numAttrs = 1;
     }
-    PLK_CUDA(cudaLaunchKernelEx(&lc, k_batch_engine<T, NT>, a));
+    PLK_CUDA(cudaLaunchKernelEx(&lc, k_batch_engine<T, NT, MINB>, a));
     return PLK_OK;
 }
 
 static int cfg_key(const BatchConfig &c) {
-    return ((c.cluster * 1024 + c.threads) * 64 + c.smem_bits) * 64 + c.cluster_min_qubits;
+    return (((c.cluster * 4 + c.ctas_per_sm) * 1024 + c.threads) * 64 + c.smem_bits) * 64 + c.cluster_min_qubits;
 }
 
-// 512-thread CTAs halve the register budget (128 per thread) and spill the
-// 32 window amplitudes; only 256-thread CTAs are built.
-constexpr bool kBuild512 = false;
-template <class T> static bool use512(const plk_batch b) { return sizeof(T) == 4 && b->cfg.threads == 512; }
+
 
 template <class T> static int prepare_run(plk_batch b) {
     if (!b->compiled) {
@@ -1078,11 +1084,11 @@ template <class T> static int prepare_run(plk_batch b) {
     if (b->lp_key == cfg_key(b->cfg)) return PLK_OK;
     LaunchPlan &lp = b->lp;
     lp = LaunchPlan();
-    if constexpr (sizeof(T) == 4 && kBuild512) {
-        if (use512<T>(b)) PLK_TRY((plan_launch<T, 512>(b, lp)));
-        else PLK_TRY((plan_launch<T, 256>(b, lp)));
+    if constexpr (sizeof(T) == 4) {
+        if (b->cfg.ctas_per_sm == 2) PLK_TRY((plan_launch<T, 256, 2>(b, lp)));
+        else PLK_TRY((plan_launch<T, 256, 1>(b, lp)));
     } else {
-        PLK_TRY((plan_launch<T, 256>(b, lp)));
+        PLK_TRY((plan_launch<T, 256, 1>(b, lp)));
     }
     // order and scratch for this configuration
     PLK_CUDA(cudaMemcpyAsync(b->d_order, lp.order.data(), lp.order.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
@@ -1110,11 +1116,11 @@ template <class T> static int enqueue_run(plk_batch b, const double *d_params, c
                                                              d_params, (c2_t<T> *)b->d_mats);
         PLK_CHECK_LAUNCH();
     }
-    if constexpr (sizeof(T) == 4 && kBuild512) {
-        if (use512<T>(b)) PLK_TRY((launch_engine<T, 512>(b, lp, st)));
-        else PLK_TRY((launch_engine<T, 256>(b, lp, st)));
+    if constexpr (sizeof(T) == 4) {
+        if (b->cfg.ctas_per_sm == 2) PLK_TRY((launch_engine<T, 256, 2>(b, lp, st)));
+        else PLK_TRY((launch_engine<T, 256, 1>(b, lp, st)));
     } else {
-        PLK_TRY((launch_engine<T, 256>(b, lp, st)));
+        PLK_TRY((launch_engine<T, 256, 1>(b, lp, st)));
     }
     return PLK_OK;
 }
@@ -1454,15 +1460,29 @@ PLK_API int plk_batch_set_config(plk_batch b, int32_t cluster, int32_t threads, 
     if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
     if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8)
         PLK_FAIL(PLK_ERR_INVALID_ARG, "cluster must be 1, 2, 4 or 8");
-    if (threads != 256 && (threads != 512 || !kBuild512)) PLK_FAIL(PLK_ERR_INVALID_ARG, "threads must be 256");
-    const int maxsb = b->dtype == PLK_C64 ? 13 : 12;
+    if (threads != 256) PLK_FAIL(PLK_ERR_INVALID_ARG, "threads must be 256");
+    const int maxsb = b->dtype == PLK_C64 && b->cfg.ctas_per_sm == 1 ? 13 : 12;
     if (smem_qubits < kWinBits || smem_qubits > maxsb)
         PLK_FAIL(PLK_ERR_INVALID_ARG, "smem_qubits must be 4.." + std::to_string(maxsb));
-    if (b->dtype == PLK_C128 && threads != 256) PLK_FAIL(PLK_ERR_INVALID_ARG, "complex128 batches use 256 threads");
     b->cfg.cluster = cluster;
     b->cfg.threads = threads;
     b->cfg.smem_bits = smem_qubits;
     b->cfg.cluster_min_qubits = cluster_min_qubits;
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_set_occupancy(plk_batch b, int32_t ctas_per_sm) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (ctas_per_sm != 1 && ctas_per_sm != 2) PLK_FAIL(PLK_ERR_INVALID_ARG, "ctas_per_sm must be 1 or 2");
+    if (ctas_per_sm == 2 && b->dtype != PLK_C64) PLK_FAIL(PLK_ERR_UNSUPPORTED, "two CTAs per SM need complex64");
+    b->cfg.ctas_per_sm = ctas_per_sm;
+    b->cfg.smem_bits = std::min(b->cfg.smem_bits, ctas_per_sm == 2 ? 12 : 13);
+    return PLK_OK;
+}
+
+PLK_API int plk_batch_get_occupancy(plk_batch b, int32_t *ctas_per_sm) {
+    if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
+    if (ctas_per_sm) *ctas_per_sm = b->cfg.ctas_per_sm;
     return PLK_OK;
 }
 
@@ -1486,7 +1506,6 @@ PLK_API int plk_batch_run(plk_batch b, double *expvals, double *jac) {
     if (!b) PLK_FAIL(PLK_ERR_INVALID_ARG, "null batch");
     if (b->circs.empty()) PLK_FAIL(PLK_ERR_INVALID_ARG, "empty batch");
     PLK_CUDA(cudaSetDevice(b->device));
-    if (b->dtype == PLK_C128 && b->cfg.threads != 256) b->cfg.threads = 256;
     return b->dtype == PLK_C64 ? run_host<float>(b, expvals, jac) : run_host<double>(b, expvals, jac);
 }
 
@@ -1495,7 +1514,6 @@ PLK_API int plk_batch_run_device(plk_batch b, const double *d_params, double *d_
     if (b->circs.empty()) PLK_FAIL(PLK_ERR_INVALID_ARG, "empty batch");
     PLK_CUDA(cudaSetDevice(b->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
-    if (b->dtype == PLK_C128 && b->cfg.threads != 256) b->cfg.threads = 256;
     return b->dtype == PLK_C64 ? run_device<float>(b, d_params, d_expvals, d_jac, st)
                                : run_device<double>(b, d_params, d_expvals, d_jac, st);
 }
@@ -1516,19 +1534,20 @@ PLK_API int plk_batch_tune(plk_batch b, int32_t reps, char *report, int32_t repo
     reps = std::max(1, reps);
     const BatchConfig saved = b->cfg;
     std::vector<BatchConfig> cands;
-    const int maxsb = b->dtype == PLK_C64 ? 13 : 12;
     int max_nq = 0;
     for (auto &c : b->circs) max_nq = std::max(max_nq, c.nq);
-    for (int threads : {256, 512}) {
-        if ((b->dtype == PLK_C128 || !kBuild512) && threads != 256) continue;
+    for (int ctas : {1, 2}) {
+        if (ctas == 2 && b->dtype != PLK_C64) continue;
+        const int sb = b->dtype == PLK_C64 && ctas == 1 ? 13 : 12;
         for (int cl : {1, 2, 4, 8}) {
-            for (int cmin : {maxsb + 1, maxsb + 3, maxsb + 5}) {
-                if (cl == 1 && cmin != maxsb + 1) continue;
+            for (int cmin : {sb + 1, sb + 3, sb + 5}) {
+                if (cl == 1 && cmin != sb + 1) continue;
                 if (cl > 1 && cmin > max_nq) continue;
                 BatchConfig c;
-                c.threads = threads;
+                c.threads = 256;
+                c.ctas_per_sm = ctas;
                 c.cluster = cl;
-                c.smem_bits = maxsb;
+                c.smem_bits = sb;
                 c.cluster_min_qubits = cmin;
                 cands.push_back(c);
             }
@@ -1541,7 +1560,7 @@ PLK_API int plk_batch_tune(plk_batch b, int32_t reps, char *report, int32_t repo
         b->cfg = c;
         int st = plk_batch_run(b, nullptr, nullptr); // warm-up (and graph capture)
         if (st != PLK_OK) {
-            rep += "cluster=" + std::to_string(c.cluster) + " threads=" + std::to_string(c.threads) +
+            rep += "ctas_per_sm=" + std::to_string(c.ctas_per_sm) + " cluster=" + std::to_string(c.cluster) +
                    " cluster_min=" + std::to_string(c.cluster_min_qubits) + " failed: " + last_error() + "\n";
             continue;
         }
@@ -1553,8 +1572,8 @@ PLK_API int plk_batch_tune(plk_batch b, int32_t reps, char *report, int32_t repo
         std::sort(t.begin(), t.end());
         const double med = t[t.size() / 2];
         char line[160];
-        std::snprintf(line, sizeof(line), "cluster=%d threads=%d smem_qubits=%d cluster_min=%d: %.3f ms\n", c.cluster,
-                      c.threads, c.smem_bits, c.cluster_min_qubits, med);
+        std::snprintf(line, sizeof(line), "ctas_per_sm=%d cluster=%d smem_qubits=%d cluster_min=%d: %.3f ms\n",
+                      c.ctas_per_sm, c.cluster, c.smem_bits, c.cluster_min_qubits, med);
         rep += line;
         if (med < best) {
             best = med;

@@ -208,12 +208,12 @@ template <class T> __device__ __forceinline__ uint32_t swz(uint32_t l) {
 
 // Global states are read and written at L2 (ld.global.cg / st.global.cg):
 // the CTAs of a cluster share them, and L1 is not coherent across SMs.
-template <class T, int MODE> __device__ __forceinline__ c2_t<T> eld(const c2_t<T> *p, uint64_t i) {
-    if constexpr (MODE == EM_SMEM) return p[swz<T>((uint32_t)i)];
+template <class T, int MODE> __device__ __forceinline__ c2_t<T> eld(const c2_t<T> *p, uint32_t i) {
+    if constexpr (MODE == EM_SMEM) return p[swz<T>(i)];
     else return __ldcg(p + i);
 }
-template <class T, int MODE> __device__ __forceinline__ void est(c2_t<T> *p, uint64_t i, c2_t<T> v) {
-    if constexpr (MODE == EM_SMEM) p[swz<T>((uint32_t)i)] = v;
+template <class T, int MODE> __device__ __forceinline__ void est(c2_t<T> *p, uint32_t i, c2_t<T> v) {
+    if constexpr (MODE == EM_SMEM) p[swz<T>(i)] = v;
     else __stcg(p + i, v);
 }
 
@@ -428,9 +428,9 @@ template <int C, int TG, class V> __device__ __forceinline__ void cx_apply(V (&v
 }
 
 // gate-local index of amplitude `idx` for a DIAG op (wire j -> bit K-1-j)
-__device__ __forceinline__ uint32_t diag_index(uint64_t idx, uint32_t bits, int K) {
+__device__ __forceinline__ uint32_t diag_index(uint32_t idx, uint32_t bits, int K) {
     uint32_t g = 0;
-    for (int j = 0; j < K; j++) g = (g << 1) | (uint32_t)((idx >> ((bits >> (5 * j)) & 31u)) & 1u);
+    for (int j = 0; j < K; j++) g = (g << 1) | ((idx >> ((bits >> (5 * j)) & 31u)) & 1u);
     return g;
 }
 

@@ -113,6 +113,8 @@ _SIGS = {
     "plk_batch_set_config": ([_vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32], C.c_int),
     "plk_batch_get_config": ([_vp, _i32p, _i32p, _i32p, _i32p], C.c_int),
     "plk_batch_set_graph": ([_vp, C.c_int32], C.c_int),
+    "plk_batch_set_occupancy": ([_vp, C.c_int32], C.c_int),
+    "plk_batch_get_occupancy": ([_vp, _i32p], C.c_int),
     "plk_batch_tune": ([_vp, C.c_int32, C.c_char_p, C.c_int32], C.c_int),
 }
 for _name, (_args, _res) in _SIGS.items():

@@ -48,31 +48,59 @@ class CircuitBatch:
 
     __del__ = close
 
+    _OP_DTYPE = np.dtype([("gate", "<i4"), ("nw", "<i4"), ("adj", "<i4"), ("np", "<i4"), ("w", "<u8"), ("p", "<u8"),
+                          ("m", "<u8")])
+
     def add(self, num_qubits: int, ops: Sequence, observable: Sequence, trainable: Sequence[int] | None = None) -> int:
-        keep = []
-        arr = (N.PlkOp * max(1, len(ops)))()
-        for i, op in enumerate(ops):
-            name, wires = op[0], op[1]
-            inv = bool(op[2]) if len(op) > 2 else False
-            prm = np.ascontiguousarray(np.asarray(op[3] if len(op) > 3 else [], dtype=np.float64).reshape(-1))
-            w = np.ascontiguousarray(np.asarray(wires, dtype=np.int64).reshape(-1))
-            mat = None
-            if name == "Matrix":
-                m = np.ascontiguousarray(np.asarray(op[4], dtype=np.complex128))
-                mat = m.view(np.float64)
-                keep.append(mat)
-            keep += [prm, w]
-            arr[i] = N.PlkOp(N.GATE_ID[name], len(w), int(inv), len(prm), _p(w, _i64p),
-                             _p(prm, _dp) if len(prm) else None, _p(mat, _dp) if mat is not None else None)
+        """Adds a circuit given as an op list; returns its index."""
+        wl = [op[1] for op in ops]
+        pl = [op[3] if len(op) > 3 else () for op in ops]
+        pk = {"gates": np.array([N.GATE_ID[op[0]] for op in ops], dtype=np.int32),
+              "wire_offsets": np.concatenate([[0], np.cumsum([len(w) for w in wl])]).astype(np.int64),
+              "wires": np.array([int(x) for w in wl for x in w], dtype=np.int64),
+              "inverse": np.array([bool(op[2]) if len(op) > 2 else False for op in ops], dtype=np.int32),
+              "param_offsets": np.concatenate([[0], np.cumsum([len(p) for p in pl])]).astype(np.int64),
+              "params": np.array([float(x) for p in pl for x in p], dtype=np.float64),
+              "matrices": {i: op[4] for i, op in enumerate(ops) if op[0] == "Matrix"}}
+        return self.add_packed(num_qubits, pk, observable, trainable)
+
+    def add_packed(self, num_qubits: int, pk: dict, observable: Sequence, trainable: Sequence[int] | None = None) -> int:
+        """Adds a circuit given as flat arrays (see circuits.layered_ansatz_arrays)."""
+        gates = np.ascontiguousarray(pk["gates"], dtype=np.int32)
+        nops = len(gates)
+        wo = np.asarray(pk["wire_offsets"], dtype=np.int64)
+        po = np.asarray(pk["param_offsets"], dtype=np.int64)
+        wires_all = np.ascontiguousarray(pk["wires"], dtype=np.int64)
+        params_all = np.ascontiguousarray(pk["params"], dtype=np.float64)
+        if len(wires_all) == 0:
+            wires_all = np.zeros(1, dtype=np.int64)
+        if len(params_all) == 0:
+            params_all = np.zeros(1, dtype=np.float64)
+        keep = [wires_all, params_all]
+        arr = np.zeros(max(1, nops), dtype=self._OP_DTYPE)
+        if nops:
+            npar = np.diff(po)
+            arr["gate"][:nops] = gates
+            arr["nw"][:nops] = np.diff(wo)
+            arr["adj"][:nops] = np.asarray(pk["inverse"], dtype=np.int32)
+            arr["np"][:nops] = npar
+            arr["w"][:nops] = wires_all.ctypes.data + 8 * wo[:-1].astype(np.uint64)
+            arr["p"][:nops] = np.where(npar > 0, params_all.ctypes.data + 8 * po[:-1].astype(np.uint64), 0)
+            for i, m in pk.get("matrices", {}).items():
+                mm = np.ascontiguousarray(np.asarray(m, dtype=np.complex128))
+                keep.append(mm)
+                arr["m"][i] = mm.ctypes.data
         coeffs = np.ascontiguousarray([float(c) for c, _, _ in observable], dtype=np.float64)
         offs = np.ascontiguousarray(np.cumsum([0] + [len(w) for _, w, _ in observable]), dtype=np.int64)
         wires = np.ascontiguousarray([x for _, w, _ in observable for x in w] or [0], dtype=np.int64)
         letters = "".join(l for _, _, l in observable).encode()
         tp = None if trainable is None else np.ascontiguousarray(trainable, dtype=np.int64)
         idx = C.c_int64()
-        N.check(N.lib.plk_batch_add(self._h, num_qubits, arr, len(ops), _p(tp, _i64p) if tp is not None else None,
-                                    0 if tp is None else len(tp), len(coeffs), _p(coeffs, _dp), _p(offs, _i64p),
-                                    _p(wires, _i64p), letters, C.byref(idx)))
+        N.check(N.lib.plk_batch_add(self._h, num_qubits, C.cast(arr.ctypes.data, C.POINTER(N.PlkOp)), nops,
+                                    _p(tp, _i64p) if tp is not None else None, 0 if tp is None else len(tp),
+                                    len(coeffs), _p(coeffs, _dp), _p(offs, _i64p), _p(wires, _i64p), letters,
+                                    C.byref(idx)))
+        del keep
         self.num_circuits += 1
         return idx.value
 
@@ -113,15 +141,18 @@ class CircuitBatch:
         N.check(N.lib.plk_batch_last_time(self._h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
-    def set_config(self, cluster=8, threads=256, smem_qubits=None, cluster_min_qubits=17):
+    def set_config(self, cluster=8, threads=256, smem_qubits=None, cluster_min_qubits=17, ctas_per_sm=1):
+        N.check(N.lib.plk_batch_set_occupancy(self._h, ctas_per_sm))
         if smem_qubits is None:
-            smem_qubits = 13 if self.dtype == "c64" else 12
+            smem_qubits = 13 if self.dtype == "c64" and ctas_per_sm == 1 else 12
         N.check(N.lib.plk_batch_set_config(self._h, cluster, threads, smem_qubits, cluster_min_qubits))
 
     def get_config(self):
-        v = [C.c_int32() for _ in range(4)]
-        N.check(N.lib.plk_batch_get_config(self._h, *[C.byref(x) for x in v]))
-        return dict(zip(("cluster", "threads", "smem_qubits", "cluster_min_qubits"), [x.value for x in v]))
+        v = [C.c_int32() for _ in range(5)]
+        N.check(N.lib.plk_batch_get_config(self._h, *[C.byref(x) for x in v[:4]]))
+        N.check(N.lib.plk_batch_get_occupancy(self._h, C.byref(v[4])))
+        return dict(zip(("cluster", "threads", "smem_qubits", "cluster_min_qubits", "ctas_per_sm"),
+                        [x.value for x in v]))
 
     def set_graph(self, use: bool) -> None:
         N.check(N.lib.plk_batch_set_graph(self._h, int(use)))

@@ -96,20 +96,65 @@ def random_pauli_words(nq: int, count: int, seed: int, max_weight: int = 4):
     return words
 
 
-def batch_workload(num_circuits: int = 4096, seed: int = 5, min_qubits: int = 8, max_qubits: int = 20,
-                   min_layers: int = 5, max_layers: int = 30, terms: int = 10):
+def layered_ansatz_arrays(nq: int, angles: np.ndarray, rotations=("RX", "RY", "RZ")):
+    """Packed form of hardware_efficient_ansatz with a CNOT ladder: angles has
+    shape (layers, nq, len(rotations)).  Returns a dict of flat arrays (gate
+    ids, wires with offsets, inverse flags, parameters with offsets)."""
+    from ._native import GATE_ID
+
+    layers, nr = angles.shape[0], len(rotations)
+    per_layer = nq * nr + (nq - 1)
+    rot_ids = np.array([GATE_ID[r] for r in rotations], dtype=np.int32)
+    gates = np.empty((layers, per_layer), dtype=np.int32)
+    gates[:, :nq * nr] = np.tile(rot_ids, nq)
+    gates[:, nq * nr:] = GATE_ID["CNOT"]
+    nw = np.ones((layers, per_layer), dtype=np.int64)
+    nw[:, nq * nr:] = 2
+    rot_w = np.repeat(np.arange(nq), nr)
+    cn_w = np.stack([np.arange(nq - 1), np.arange(1, nq)], axis=1).reshape(-1)
+    wires = np.tile(np.concatenate([rot_w, cn_w]), layers).astype(np.int64)
+    npar = np.zeros((layers, per_layer), dtype=np.int64)
+    npar[:, :nq * nr] = 1
+    return {"gates": gates.reshape(-1), "wire_offsets": np.concatenate([[0], np.cumsum(nw)]).astype(np.int64),
+            "wires": wires, "inverse": np.zeros(gates.size, dtype=np.int32),
+            "param_offsets": np.concatenate([[0], np.cumsum(npar)]).astype(np.int64),
+            "params": np.ascontiguousarray(angles, dtype=np.float64).reshape(-1)}
+
+
+def packed_to_ops(pk):
+    """[(name, wires, inverse, params)] from the packed form."""
+    from ._native import GATES
+
+    g, wo, w, inv, po, p = (pk["gates"], pk["wire_offsets"], pk["wires"], pk["inverse"], pk["param_offsets"],
+                            pk["params"])
+    return [(GATES[g[i]], [int(x) for x in w[wo[i]:wo[i + 1]]], bool(inv[i]), [float(x) for x in p[po[i]:po[i + 1]]])
+            for i in range(len(g))]
+
+
+def batch_workload_packed(num_circuits: int = 4096, seed: int = 5, min_qubits: int = 8, max_qubits: int = 20,
+                          min_layers: int = 5, max_layers: int = 30, terms: int = 10):
     """Independent circuits of uneven size: qubits uniform in [min_qubits,
     max_qubits], depth uniform in [min_layers, max_layers] layers of RX, RY,
     RZ on every wire plus a CNOT ladder, angles uniform in [0, 2*pi), and a
-    `terms`-word random Pauli Hamiltonian per circuit.
-    Returns [(num_qubits, ops, words)]."""
+    `terms`-word Pauli Hamiltonian per circuit (weight uniform in 1..4,
+    distinct uniform wires, letters uniform in X/Y/Z, N(0, 1) coefficients).
+    Returns [(num_qubits, packed ops, words)]."""
     rng = np.random.default_rng(seed)
+    nqs = rng.integers(min_qubits, max_qubits + 1, size=num_circuits)
+    depths = rng.integers(min_layers, max_layers + 1, size=num_circuits)
     out = []
-    for _ in range(num_circuits):
-        nq = int(rng.integers(min_qubits, max_qubits + 1))
-        layers = int(rng.integers(min_layers, max_layers + 1))
-        sub = int(rng.integers(0, 2**31 - 1))
-        ops = hardware_efficient_ansatz(nq, layers, sub, rotations=("RX", "RY", "RZ"), entangler="ladder")
-        words = random_pauli_words(nq, terms, sub + 1)
-        out.append((nq, ops, words))
+    for nq, d in zip(nqs, depths):
+        nq, d = int(nq), int(d)
+        angles = rng.uniform(0, 2 * np.pi, size=(d, nq, 3))
+        words = []
+        for _ in range(terms):
+            k = int(rng.integers(1, min(4, nq) + 1))
+            w = [int(x) for x in rng.choice(nq, size=k, replace=False)]
+            words.append((float(rng.normal()), w, "".join(rng.choice(list("XYZ"), size=k))))
+        out.append((nq, layered_ansatz_arrays(nq, angles), words))
     return out
+
+
+def batch_workload(num_circuits: int = 4096, seed: int = 5, **kw):
+    """batch_workload_packed as [(num_qubits, ops, words)] op lists."""
+    return [(nq, packed_to_ops(pk), words) for nq, pk, words in batch_workload_packed(num_circuits, seed, **kw)]

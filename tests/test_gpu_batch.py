@@ -127,6 +127,13 @@ def test_batch_placements_c128(config):
     check_against_oracle(SMALL, ev, grads, 1e-10)
 
 
+def test_batch_two_ctas_per_sm_c64():
+    cases = SMALL + make_cases("two", [13, 14, 11], 40)
+    for cfg in (dict(cluster=1, ctas_per_sm=2), dict(cluster=4, ctas_per_sm=2, cluster_min_qubits=13)):
+        ev, grads = run_batch(cases, "c64", cfg)
+        check_against_oracle(cases, ev, grads, 1e-4)
+
+
 def test_batch_larger_circuits_clusters():
     cases = make_cases("large", [13, 14, 15, 16, 12, 14], 60)
     for dtype, tol, sq in (("c128", 1e-10, 12), ("c64", 1e-4, 13)):
