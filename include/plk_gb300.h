@@ -243,6 +243,13 @@ PLK_API int plk_adjoint_jacobian_inplace(plk_state lambda, plk_state *hlambda, i
 PLK_API int plk_expval_pauliz_noalloc(const void *state, int32_t num_qubits, int32_t dtype, int32_t count,
                                       const int64_t *wires, double *out, void *cuda_stream);
 
+/* ---- register-window path ----------------------------------------------- */
+/* complex64 op lists (plk_apply_ops) and one-observable adjoint Jacobians run
+ * as register-window sweeps (about seven ops per state pass) unless this is
+ * switched off; results agree with the op-at-a-time path to rounding. */
+PLK_API int plk_set_window_path(int32_t enable);
+PLK_API int plk_get_window_path(int32_t *enabled);
+
 /* ---- gate matrices ---------------------------------------------------- */
 /* Dense matrix (row-major complex128 pairs, 4^num_wires of them; wires[0] is
  * the most significant bit of the row index) of a named gate, built from the

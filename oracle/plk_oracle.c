@@ -104,8 +104,11 @@ static void sort_small(int *a, int m) {
     }
 }
 
+/* wire lists hold at most ORC_MAX_QUBITS entries (every wire of the state) */
+#define ORC_MAX_QUBITS 40
+
 static int check_wires(int nq, const int64_t *wires, int nw) {
-    if (nq < 1 || nq > 40 || nw < 1 || nw > nq) return ORC_BAD_ARGS;
+    if (nq < 1 || nq > ORC_MAX_QUBITS || nw < 1 || nw > nq) return ORC_BAD_ARGS;
     for (int i = 0; i < nw; i++) {
         if (wires[i] < 0 || wires[i] >= nq) return ORC_BAD_ARGS;
         for (int j = 0; j < i; j++)
@@ -211,7 +214,7 @@ int orc_apply(orc_cplx *a, int nq, const char *name, const int64_t *wires,
     if (check_wires(nq, wires, nw) != ORC_OK) return ORC_BAD_ARGS;
     if (np < gate_nparams(kind)) return ORC_BAD_ARGS;
     const double th = (np > 0) ? params[0] : 0.0;
-    int rev[8];
+    int rev[ORC_MAX_QUBITS];
     rev_wires(nq, wires, nw, rev);
 
     if (kind == G_MRZ) {
@@ -470,7 +473,7 @@ int orc_apply(orc_cplx *a, int nq, const char *name, const int64_t *wires,
 int orc_apply_matrix(orc_cplx *a, int nq, const orc_cplx *mat,
                      const int64_t *wires, int nw, int inverse) {
     if (check_wires(nq, wires, nw) != ORC_OK || nw > 12) return ORC_BAD_ARGS;
-    int rev[16];
+    int rev[ORC_MAX_QUBITS];
     rev_wires(nq, wires, nw, rev);
     const uint64_t dim = (uint64_t)1 << nw;
     if (nw == 1) {
@@ -645,7 +648,7 @@ double orc_apply_generator(orc_cplx *a, int nq, const char *name,
         *status = ORC_BAD_ARGS;
         return 0.0;
     }
-    int rev[8];
+    int rev[ORC_MAX_QUBITS];
     rev_wires(nq, wires, nw, rev);
     const orc_cplx Z0 = C(0.0, 0.0), PI_ = C(0.0, 1.0), MI_ = C(0.0, -1.0);
     if (kind == G_MRZ) {

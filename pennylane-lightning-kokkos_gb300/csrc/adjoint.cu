@@ -28,6 +28,8 @@ int plan_gate(int gate, int nw, bool inv, const double *prm, int np, GatePlan &p
 int plan_generator(int gate, int nw, GatePlan &p);
 int apply_gate_impl(plk_state s, int gate, const int64_t *wires, int nw, bool adj, const double *params, int np,
                     const double *matrix);
+int window_adjoint(plk_state lam, plk_state hl, const plk_op *ops, int nops, const int64_t *tp, int ntp, double *jac,
+                   bool &handled);
 
 enum AdjKind : int {
     A_RX = 0, A_RY, A_RZ, A_PS, A_CRX, A_CRY, A_CRZ, A_CPS, A_IXX, A_IXY, A_IYY, A_IZZ,
@@ -490,7 +492,9 @@ static int adjoint_run(plk_state work, plk_state *hlambda, int32_t nobs, const p
         old_streams[o] = hlambda[o]->stream;
         st = plk_state_set_stream(hlambda[o], work->stream);
     }
-    if (st == PLK_OK)
+    bool handled = false;
+    if (st == PLK_OK && nobs == 1) st = window_adjoint(work, hlambda[0], ops, nops, trainable, ntp, jac, handled);
+    if (st == PLK_OK && !handled)
         st = work->dtype == PLK_C64 ? adjoint_impl<float>(work, hlambda, nobs, ops, nops, trainable, ntp, jac)
                                     : adjoint_impl<double>(work, hlambda, nobs, ops, nops, trainable, ntp, jac);
     const std::string err = st == PLK_OK ? std::string() : last_error();

@@ -29,192 +29,9 @@
 #include <string>
 #include <vector>
 
-#include "batch_engine.cuh"
-#include "gate_ops.cuh"
+#include "window_host.cuh"
 
 namespace plk {
-
-int plan_gate(int gate, int nw, bool inv, const double *prm, int np, GatePlan &p);
-int plan_generator(int gate, int nw, GatePlan &p);
-
-// ------------------------------------------------------- dense gate plans --
-// Applies a plan to the local amplitudes v[0 .. 2^K) (bit K-1-j <-> wires[j]).
-static void apply_plan_host(const GatePlan &p, int K, double2 *v) {
-    const int D = 1 << K;
-    switch (p.family) {
-    case GatePlan::F_NOOP: return;
-    case GatePlan::F_PAIR: {
-        double2 &x = v[p.a], &y = v[p.b];
-        switch (p.op) {
-        case P_SWAP: pair_op<P_SWAP>(x, y, p.coef); break;
-        case P_Y: pair_op<P_Y>(x, y, p.coef); break;
-        case P_H: pair_op<P_H>(x, y, p.coef); break;
-        case P_RX: pair_op<P_RX>(x, y, p.coef); break;
-        case P_RY: pair_op<P_RY>(x, y, p.coef); break;
-        case P_MAT: pair_op<P_MAT>(x, y, p.coef); break;
-        case P_DIAG: pair_op<P_DIAG>(x, y, p.coef); break;
-        case P_PHASE_Y: pair_op<P_PHASE_Y>(x, y, p.coef); break;
-        case P_ZERO: pair_op<P_ZERO>(x, y, p.coef); break;
-        case P_GEN_SWAPI: pair_op<P_GEN_SWAPI>(x, y, p.coef); break;
-        case P_ZERO_Y: pair_op<P_ZERO_Y>(x, y, p.coef); break;
-        case P_NEG_Y: pair_op<P_NEG_Y>(x, y, p.coef); break;
-        case P_MULI_Y: pair_op<P_MULI_Y>(x, y, p.coef); break;
-        default: break;
-        }
-        for (int i = 0; i < p.n_extra; i++) {
-            double2 &e = v[p.extra_idx[i]];
-            if (p.extra_mode == X_PHASE) e = cmul(e, mk<double2>(p.extra_e[0], p.extra_e[1]));
-            else if (p.extra_mode == X_ZERO) e = mk<double2>(0, 0);
-        }
-        return;
-    }
-    case GatePlan::F_QUAD: {
-        double2 q[4] = {v[0], v[1], v[2], v[3]};
-        switch (p.op) {
-        case Q_IXX: quad_op<Q_IXX>(q, p.coef); break;
-        case Q_IYY: quad_op<Q_IYY>(q, p.coef); break;
-        case Q_DIAG: quad_op<Q_DIAG>(q, p.coef); break;
-        case Q_MAT: quad_op<Q_MAT>(q, p.coef); break;
-        case Q_GEN_IXX: quad_op<Q_GEN_IXX>(q, p.coef); break;
-        case Q_GEN_IYY: quad_op<Q_GEN_IYY>(q, p.coef); break;
-        default: break;
-        }
-        for (int i = 0; i < 4; i++) v[i] = q[i];
-        return;
-    }
-    case GatePlan::F_MRZ:
-        for (int i = 0; i < D; i++) {
-            const bool odd = __builtin_popcount((unsigned)i) & 1;
-            v[i] = cmul(v[i], odd ? mk<double2>(p.coef[2], p.coef[3]) : mk<double2>(p.coef[0], p.coef[1]));
-        }
-        return;
-    case GatePlan::F_GEN_MRZ:
-        for (int i = 0; i < D; i++)
-            if (__builtin_popcount((unsigned)i) & 1) v[i] = cneg(v[i]);
-        return;
-    default: return;
-    }
-}
-
-static void plan_dense(const GatePlan &p, int K, std::vector<double2> &M) {
-    const int D = 1 << K;
-    M.assign((size_t)D * D, mk<double2>(0, 0));
-    std::vector<double2> v(D);
-    for (int c = 0; c < D; c++) {
-        std::fill(v.begin(), v.end(), mk<double2>(0, 0));
-        v[c] = mk<double2>(1, 0);
-        apply_plan_host(p, K, v.data());
-        for (int r = 0; r < D; r++) M[(size_t)r * D + c] = v[r];
-    }
-}
-
-static int gate_dense(int gate, int K, bool inv, double theta, std::vector<double2> &M) {
-    GatePlan p;
-    const double prm[3] = {theta, 0.0, 0.0};
-    PLK_TRY(plan_gate(gate, K, inv, prm, 3, p));
-    plan_dense(p, p.family == GatePlan::F_NOOP ? K : (p.K > 0 ? p.K : K), M);
-    return PLK_OK;
-}
-
-static void trig5(double th, double *f) {
-    f[0] = 1.0;
-    f[1] = std::cos(th / 2);
-    f[2] = std::sin(th / 2);
-    f[3] = std::cos(th);
-    f[4] = std::sin(th);
-}
-
-// Coefficient matrices A0..A4 of U(theta) (D*D complex each).
-static int fit_gate(int gate, int K, bool inv, int nparams, std::vector<double2> &A) {
-    const int D = 1 << K;
-    const size_t DD = (size_t)D * D;
-    A.assign(5 * DD, mk<double2>(0, 0));
-    std::vector<double2> U;
-    if (nparams == 0) {
-        PLK_TRY(gate_dense(gate, K, inv, 0.0, U));
-        std::copy(U.begin(), U.end(), A.begin());
-        return PLK_OK;
-    }
-    static const double th[5] = {0.37, 1.61, 2.83, 4.07, 5.51};
-    double F[5][5];
-    std::vector<std::vector<double2>> R(5);
-    for (int k = 0; k < 5; k++) {
-        trig5(th[k], F[k]);
-        PLK_TRY(gate_dense(gate, K, inv, th[k], R[k]));
-    }
-    // Gaussian elimination with partial pivoting on F, applied to every entry
-    int perm[5] = {0, 1, 2, 3, 4};
-    for (int c = 0; c < 5; c++) {
-        int piv = c;
-        for (int r = c + 1; r < 5; r++)
-            if (std::fabs(F[r][c]) > std::fabs(F[piv][c])) piv = r;
-        if (piv != c) {
-            for (int j = 0; j < 5; j++) std::swap(F[c][j], F[piv][j]);
-            std::swap(R[c], R[piv]);
-            std::swap(perm[c], perm[piv]);
-        }
-        for (int r = c + 1; r < 5; r++) {
-            const double f = F[r][c] / F[c][c];
-            for (int j = c; j < 5; j++) F[r][j] -= f * F[c][j];
-            for (size_t e = 0; e < DD; e++) {
-                R[r][e].x -= f * R[c][e].x;
-                R[r][e].y -= f * R[c][e].y;
-            }
-        }
-    }
-    for (int i = 4; i >= 0; i--) {
-        for (size_t e = 0; e < DD; e++) {
-            double re = R[i][e].x, im = R[i][e].y;
-            for (int j = i + 1; j < 5; j++) {
-                re -= F[i][j] * A[j * DD + e].x;
-                im -= F[i][j] * A[j * DD + e].y;
-            }
-            A[i * DD + e] = mk<double2>(re / F[i][i], im / F[i][i]);
-        }
-    }
-    for (auto &z : A) {
-        if (std::fabs(z.x) < 1e-15) z.x = 0.0;
-        if (std::fabs(z.y) < 1e-15) z.y = 0.0;
-    }
-    // check the fit at angles it was not fitted on
-    for (double t : {0.9, 3.3, -2.2}) {
-        double f[5];
-        trig5(t, f);
-        PLK_TRY(gate_dense(gate, K, inv, t, U));
-        for (size_t e = 0; e < DD; e++) {
-            double re = 0, im = 0;
-            for (int i = 0; i < 5; i++) {
-                re += f[i] * A[i * DD + e].x;
-                im += f[i] * A[i * DD + e].y;
-            }
-            if (std::fabs(re - U[e].x) > 1e-12 || std::fabs(im - U[e].y) > 1e-12)
-                PLK_FAIL(PLK_ERR_UNSUPPORTED, "internal: gate matrix is not of degree one in theta/2");
-        }
-    }
-    return PLK_OK;
-}
-
-// -------------------------------------------------------- host structures --
-struct EPrep {
-    int32_t basis; // complex offset of the 5 coefficient blocks
-    int32_t pidx;  // flat parameter index, -1 for constant ops
-    int32_t out;   // complex offset of the output in the matrix buffer
-    uint8_t K, kind, conjT, pad;
-    uint8_t perm[4]; // DENSE: canonical bit of wires[j]
-};
-
-struct XOp { // an op after expansion (Rot -> RZ RY RZ)
-    int gate;
-    int K;
-    int wires[4];
-    std::vector<int> mrz_wires; // MultiRZ
-    bool inv;
-    int pidx;   // flat parameter index in the batch, -1 if none
-    int slot;   // Jacobian slot in the circuit, -1 if not trainable
-    int kind;   // EK_*
-    int basis;  // basis offset (complex)
-    int user_matrix; // index into the batch's user matrices, -1 if none
-};
 
 struct BatchConfig {
     int cluster = 8;        // CTAs per cluster for the largest circuits
@@ -287,15 +104,6 @@ struct plk_batch_s {
 
 namespace plk {
 
-static bool is_diag_gate(int g) {
-    switch (g) {
-    case PLK_GATE_PAULIZ: case PLK_GATE_S: case PLK_GATE_T: case PLK_GATE_PHASESHIFT: case PLK_GATE_RZ:
-    case PLK_GATE_CZ: case PLK_GATE_CONTROLLEDPHASESHIFT: case PLK_GATE_CRZ: case PLK_GATE_ISINGZZ:
-        return true;
-    default: return false;
-    }
-}
-
 static int gate_nwires(int g);
 static int gate_nparams(int g);
 
@@ -333,167 +141,6 @@ static void free_device(plk_batch b) {
     b->lp_key = -1;
 }
 
-// ----------------------------------------------------------- compilation --
-struct WinBuilder {
-    plk_batch b;
-    int nq;
-    bool bwd;
-    std::vector<EWin> &wins;
-    std::vector<EOp> &ops;
-    std::vector<ETrain> &train;
-    std::vector<EPrep> &prep;
-    std::vector<double2> &gen;
-    int64_t &n_mats;
-
-    std::vector<const XOp *> cur;
-    uint32_t wbits = 0; // state bits of the open window
-    int ntrain = 0;
-
-    static int popc(uint32_t x) { return __builtin_popcount(x); }
-
-    uint32_t need(const XOp &o) const {
-        if (o.kind == EK_DIAG || o.kind == EK_PARITY) return 0;
-        uint32_t m = 0;
-        for (int j = 0; j < o.K; j++) m |= 1u << (nq - 1 - o.wires[j]);
-        return m;
-    }
-
-    int add(const XOp &o) {
-        const uint32_t m = need(o);
-        const bool tr = bwd && o.slot >= 0;
-        if (!cur.empty() && (popc(wbits | m) > kWinBits || (int)cur.size() >= kMaxWinOps ||
-                             (tr && ntrain >= kMaxWinTrain)))
-            PLK_TRY(close());
-        cur.push_back(&o);
-        wbits |= m;
-        if (tr) ntrain++;
-        return PLK_OK;
-    }
-
-    int close() {
-        if (cur.empty()) return PLK_OK;
-        // pad with the highest unused state bits (low bits stay with the
-        // threads, which keeps global accesses coalesced)
-        uint32_t w = wbits;
-        for (int bit = nq - 1; bit >= 0 && popc(w) < kWinBits; bit--) w |= 1u << bit;
-        EWin win;
-        int r = 0;
-        int pos[32];
-        for (int bit = 0; bit < nq; bit++)
-            if (w >> bit & 1) {
-                win.rb[r] = (uint8_t)bit;
-                pos[bit] = r++;
-            }
-        win.op0 = (int)ops.size();
-        win.nops = (int)cur.size();
-        win.tr0 = (int)train.size();
-        win.ntrain = 0;
-        for (const XOp *op : cur) {
-            const XOp &o = *op;
-            EOp e;
-            std::memset(&e, 0, sizeof(e));
-            e.kind = (uint8_t)o.kind;
-            e.K = (uint8_t)o.K;
-            e.red = 0xff;
-            e.mat = -1;
-            e.gen = -1;
-            const int D = 1 << o.K;
-            uint8_t perm[4] = {0, 0, 0, 0};
-            if (o.kind == EK_CX) {
-                const int rc = pos[nq - 1 - o.wires[0]], rt = pos[nq - 1 - o.wires[1]];
-                e.sel = (uint8_t)(rc * 4 + rt);
-            } else if (o.kind == EK_DENSE) {
-                int rr[4], srt[4];
-                for (int j = 0; j < o.K; j++) srt[j] = rr[j] = pos[nq - 1 - o.wires[j]];
-                std::sort(srt, srt + o.K);
-                for (int j = 0; j < o.K; j++) perm[j] = (uint8_t)(std::find(srt, srt + o.K, rr[j]) - srt);
-                if (o.K == 1) {
-                    const int form = o.gate == PLK_GATE_RX ? EF_RX : (o.gate == PLK_GATE_RY ? EF_RY : EF_GENERAL);
-                    e.sel = (uint8_t)(srt[0] + 4 * form);
-                }
-                else if (o.K == 2) {
-                    static const int a[6] = {0, 0, 0, 1, 1, 2}, c[6] = {1, 2, 3, 2, 3, 3};
-                    for (int s = 0; s < 6; s++)
-                        if (a[s] == srt[0] && c[s] == srt[1]) e.sel = (uint8_t)s;
-                } else if (o.K == 3) {
-                    e.sel = (uint8_t)(6 - srt[0] - srt[1] - srt[2]);
-                } else {
-                    e.sel = 0;
-                }
-            } else if (o.kind == EK_DIAG) {
-                uint32_t bits = 0;
-                for (int j = 0; j < o.K; j++) bits |= (uint32_t)(nq - 1 - o.wires[j]) << (5 * j);
-                e.bits = bits;
-            } else { // parity
-                uint32_t mask = 0;
-                for (int wv : o.mrz_wires) mask |= 1u << (nq - 1 - wv);
-                e.bits = mask;
-            }
-            if (o.kind != EK_CX) {
-                EPrep p;
-                std::memset(&p, 0, sizeof(p));
-                p.basis = o.basis;
-                p.pidx = o.pidx;
-                p.out = (int32_t)n_mats;
-                p.K = (uint8_t)(o.kind == EK_PARITY ? 1 : o.K);
-                p.kind = (uint8_t)o.kind;
-                p.conjT = bwd ? 1 : 0;
-                std::memcpy(p.perm, perm, 4);
-                prep.push_back(p);
-                e.mat = (int32_t)n_mats;
-                n_mats += o.kind == EK_DENSE ? (int64_t)D * D : (o.kind == EK_DIAG ? D : 2);
-            }
-            if (bwd && o.slot >= 0) {
-                // generator (constant): canonical dense block or diagonal
-                GatePlan gp;
-                PLK_TRY(plan_generator(o.gate, o.kind == EK_PARITY ? (int)o.mrz_wires.size() : o.K, gp));
-                float gscale = (float)(-2.0 * gp.scale * (o.inv ? -1.0 : 1.0));
-                if (o.kind != EK_PARITY) {
-                    std::vector<double2> G;
-                    plan_dense(gp, o.K, G);
-                    e.gen = (int32_t)gen.size();
-                    if (o.kind == EK_DENSE && o.K == 1) {
-                        // monomial pattern (rows of G in canonical order = gate order for one wire)
-                        uint32_t pat = 0;
-                        for (int r2 = 0; r2 < 2; r2++)
-                            for (int c2 = 0; c2 < 2; c2++) {
-                                const double2 z = G[(size_t)r2 * 2 + c2];
-                                if (z.x == 0.0 && z.y == 0.0) continue;
-                                const int q = z.x == 1.0 ? 0 : z.y == 1.0 ? 1 : z.x == -1.0 ? 2 : z.y == -1.0 ? 3 : -1;
-                                if (q < 0 || (pat >> (4 * r2) & 1u))
-                                    PLK_FAIL(PLK_ERR_UNSUPPORTED, "internal: generator is not a signed permutation");
-                                pat |= (uint32_t)(1 | (c2 << 1) | (q << 2)) << (4 * r2);
-                            }
-                        e.bits = pat;
-                    }
-                    if (o.kind == EK_DENSE) {
-                        for (int r2 = 0; r2 < D; r2++)
-                            for (int c2 = 0; c2 < D; c2++) {
-                                int gr = 0, gc = 0;
-                                for (int j = 0; j < o.K; j++) {
-                                    gr |= ((r2 >> perm[j]) & 1) << (o.K - 1 - j);
-                                    gc |= ((c2 >> perm[j]) & 1) << (o.K - 1 - j);
-                                }
-                                gen.push_back(G[(size_t)gr * D + gc]);
-                            }
-                    } else { // diagonal generator
-                        for (int i = 0; i < D; i++) gen.push_back(G[(size_t)i * D + i]);
-                    }
-                }
-                e.red = (uint8_t)win.ntrain;
-                train.push_back(ETrain{o.slot, gscale});
-                win.ntrain++;
-            }
-            ops.push_back(e);
-        }
-        wins.push_back(win);
-        cur.clear();
-        wbits = 0;
-        ntrain = 0;
-        return PLK_OK;
-    }
-};
-
 static int compile_batch(plk_batch b) {
     b->h_circ.clear();
     b->h_win.clear();
@@ -517,7 +164,7 @@ static int compile_batch(plk_batch b) {
         b->h_terms.insert(b->h_terms.end(), c.terms.begin(), c.terms.end());
         for (int dir = 0; dir < 2; dir++) {
             const bool bwd = dir == 1;
-            WinBuilder wb{b, c.nq, bwd, b->h_win, b->h_ops, b->h_train, b->h_prep, b->h_gen, b->n_mats};
+            WinBuilder wb{c.nq, bwd, b->h_win, b->h_ops, b->h_train, b->h_prep, b->h_gen, b->n_mats};
             const int w0 = (int)b->h_win.size();
             const int n = (int)c.ops.size();
             if (!bwd) {
@@ -657,170 +304,6 @@ __device__ __forceinline__ void esync(int C) {
     }
 }
 
-template <class T, bool BWD>
-__device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps], c2_t<T> (&hv)[kWinAmps], uint32_t base,
-                                          const uint32_t (&bb)[4], const c2_t<T> *__restrict__ mats, EAcc<T> &acc,
-                                          EAcc<T> &acc1) {
-    using V = c2_t<T>;
-    const bool tr = BWD && op.red != 0xff;
-    if (op.kind == EK_DENSE) {
-        const V *U = mats + op.mat;
-#define PLK_DENSE1_CASE(S_)                                                                                           \
-    case 16 + S_:                                                                                                      \
-        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
-        dense_apply<1, S_>(lv, U);                                                                                     \
-        if (BWD) dense_apply<1, S_>(hv, U);                                                                            \
-        break;                                                                                                         \
-    case 16 + 4 + S_:                                                                                                  \
-        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
-        rx_apply<S_>(lv, U);                                                                                           \
-        if (BWD) rx_apply<S_>(hv, U);                                                                                  \
-        break;                                                                                                         \
-    case 16 + 8 + S_:                                                                                                  \
-        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
-        ry_apply<S_>(lv, U);                                                                                           \
-        if (BWD) ry_apply<S_>(hv, U);                                                                                  \
-        break;
-#define PLK_DENSE_CASE(K_, S_)                                                                                        \
-    case K_ * 16 + S_:                                                                                                 \
-        if (tr) dense_gen_dot<K_, S_, T>(lv, hv, mats + op.gen, acc);                                                  \
-        dense_apply<K_, S_>(lv, U);                                                                                    \
-        if (BWD) dense_apply<K_, S_>(hv, U);                                                                           \
-        break;
-        switch (op.K * 16 + op.sel) {
-            PLK_DENSE1_CASE(0) PLK_DENSE1_CASE(1) PLK_DENSE1_CASE(2) PLK_DENSE1_CASE(3)
-            PLK_DENSE_CASE(2, 0) PLK_DENSE_CASE(2, 1) PLK_DENSE_CASE(2, 2) PLK_DENSE_CASE(2, 3)
-            PLK_DENSE_CASE(2, 4) PLK_DENSE_CASE(2, 5)
-        default: {
-            // K = 3, 4: sel = missing register bit (K = 3) or 0 (K = 4)
-            // (copies keep lv / hv themselves in registers)
-            const uint32_t smask = op.K == 4 ? 15u : (15u & ~(1u << op.sel));
-            V tl[kWinAmps], th[kWinAmps];
-#pragma unroll
-            for (int j = 0; j < kWinAmps; j++) {
-                tl[j] = lv[j];
-                th[j] = hv[j];
-            }
-            if (tr) dense_gen_dot_rt<T>(tl, th, mats + op.gen, op.K, smask, acc);
-            dense_apply_rt(tl, U, op.K, smask);
-            if (BWD) dense_apply_rt(th, U, op.K, smask);
-#pragma unroll
-            for (int j = 0; j < kWinAmps; j++) {
-                lv[j] = tl[j];
-                hv[j] = th[j];
-            }
-            break;
-        }
-        }
-#undef PLK_DENSE_CASE
-#undef PLK_DENSE1_CASE
-    } else if (op.kind == EK_CX) {
-#define PLK_CX_CASE(C_, T_)                                                                                           \
-    case C_ * 4 + T_:                                                                                                  \
-        cx_apply<C_, T_>(lv);                                                                                          \
-        if (BWD) cx_apply<C_, T_>(hv);                                                                                 \
-        break;
-        switch (op.sel) {
-            PLK_CX_CASE(0, 1) PLK_CX_CASE(0, 2) PLK_CX_CASE(0, 3) PLK_CX_CASE(1, 0) PLK_CX_CASE(1, 2)
-            PLK_CX_CASE(1, 3) PLK_CX_CASE(2, 0) PLK_CX_CASE(2, 1) PLK_CX_CASE(2, 3) PLK_CX_CASE(3, 0)
-            PLK_CX_CASE(3, 1) PLK_CX_CASE(3, 2)
-        default: break;
-        }
-#undef PLK_CX_CASE
-    } else if (op.kind == EK_DIAG && op.K == 1) {
-        // one-wire diagonal (RZ, PhaseShift, Z, S, T): two phases by one bit
-        const uint32_t b0 = op.bits & 31u;
-        const V e0 = mats[op.mat], e1 = mats[op.mat + 1];
-        T g0 = 0, g1 = 0;
-        if (tr) {
-            g0 = mats[op.gen].x;
-            g1 = mats[op.gen + 1].x;
-        }
-        T t = 0;
-#pragma unroll
-        for (int j = 0; j < kWinAmps; j++) {
-            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
-                                 ((j & 8) ? bb[3] : 0);
-            const bool one = (idx >> b0) & 1u;
-            if (tr) {
-                // Im(conj(h) g v) = g (h.x v.y - h.y v.x); two amplitudes per FP32 partial
-                const T gd = one ? g1 : g0;
-                t = fma(gd * hv[j].x, lv[j].y, t);
-                t = fma(-gd * hv[j].y, lv[j].x, t);
-                if (j & 1) {
-                    ((j >> 1) & 1 ? acc1 : acc).addf(t);
-                    t = 0;
-                }
-            }
-            const V e = one ? e1 : e0;
-            lv[j] = cmul(lv[j], e);
-            if (BWD) hv[j] = cmul(hv[j], e);
-        }
-    } else {
-        const bool parity = op.kind == EK_PARITY;
-#pragma unroll
-        for (int j = 0; j < kWinAmps; j++) {
-            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
-                                 ((j & 8) ? bb[3] : 0);
-            const uint32_t g = parity ? (uint32_t)(__popc(idx & op.bits) & 1) : diag_index(idx, op.bits, op.K);
-            const V e = mats[op.mat + g];
-            if (tr) {
-                // generator diagonal: MultiRZ (-1)^parity, otherwise real entries 0, +-1
-                const T gd = parity ? (g ? (T)-1 : (T)1) : mats[op.gen + g].x;
-                (j & 1 ? acc1 : acc).im_dot(hv[j], mk<V>(gd * lv[j].x, gd * lv[j].y));
-            }
-            lv[j] = cmul(lv[j], e);
-            if (BWD) hv[j] = cmul(hv[j], e);
-        }
-    }
-}
-
-template <class T, int NT, int MODE, bool BWD>
-__device__ __noinline__ void run_window(const EngArgs<T> &a, const EWin &w, int nq, c2_t<T> *lam, c2_t<T> *hl, uint32_t t0,
-                                        uint32_t tstep, typename EAcc<T>::Slot *part) {
-    using V = c2_t<T>;
-    const int lane = threadIdx.x & 31;
-    const uint32_t nu = 1u << (nq - kWinBits);
-    const uint32_t bb[4] = {1u << w.rb[0], 1u << w.rb[1], 1u << w.rb[2], 1u << w.rb[3]};
-    for (uint32_t u = t0; u - lane < nu; u += tstep) {
-        const bool act = u < nu;
-        uint32_t base = u;
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const uint32_t lo = base & (bb[i] - 1);
-            base = ((base ^ lo) << 1) | lo;
-        }
-        V lv[kWinAmps], hv[kWinAmps];
-#pragma unroll
-        for (int j = 0; j < kWinAmps; j++) {
-            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
-                                 ((j & 8) ? bb[3] : 0);
-            lv[j] = act ? eld<T, MODE>(lam, idx) : mk<V>(0, 0);
-            if (BWD) hv[j] = act ? eld<T, MODE>(hl, idx) : mk<V>(0, 0);
-            else hv[j] = mk<V>(0, 0);
-        }
-        for (int k = 0; k < w.nops; k++) {
-            const EOp op = a.ops[w.op0 + k];
-            EAcc<T> acc, acc1;
-            if (BWD && op.red != 0xff) acc.load(part[op.red * NT + threadIdx.x]);
-            window_op<T, BWD>(op, lv, hv, base, bb, a.mats, acc, acc1);
-            if (BWD && op.red != 0xff) {
-                acc.merge(acc1);
-                part[op.red * NT + threadIdx.x] = acc.slot();
-            }
-        }
-        if (act) {
-#pragma unroll
-            for (int j = 0; j < kWinAmps; j++) {
-                const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
-                                     ((j & 8) ? bb[3] : 0);
-                est<T, MODE>(lam, idx, lv[j]);
-                if (BWD) est<T, MODE>(hl, idx, hv[j]);
-            }
-        }
-    }
-}
-
 // Per trainable op of the window: one warp sums the CTA's per-thread partials
 // in a fixed order (and clears them for the next use of the buffer).
 template <class T, int NT>
@@ -898,7 +381,7 @@ __device__ void run_circuit(const EngArgs<T> &a, int cid, int rank, int C, c2_t<
     esync(C);
     for (int k = 0; k < ci.nfw; k++) {
         const EWin w = a.win[ci.fw0 + k];
-        run_window<T, NT, MODE, false>(a, w, ci.nq, lam, hl, t0, tstep, part);
+        run_window<T, NT, MODE, false>(a.ops, a.mats, w, ci.nq, lam, hl, t0, tstep, part);
         esync(C);
     }
     h_pass<T, NT, MODE>(a, ci, lam, hl, t0, tstep, misc, rank, C);
@@ -913,7 +396,7 @@ __device__ void run_circuit(const EngArgs<T> &a, int cid, int rank, int C, c2_t<
         // two partial buffers: finalizing window k overlaps window k + 1;
         // one buffer: a barrier after finalizing
         typename EAcc<T>::Slot *rb = part + (NBUF == 2 ? (k & 1) : 0) * kMaxWinTrain * NT;
-        run_window<T, NT, MODE, true>(a, w, ci.nq, lam, hl, t0, tstep, rb);
+        run_window<T, NT, MODE, true>(a.ops, a.mats, w, ci.nq, lam, hl, t0, tstep, rb);
         esync(C);
         finalize_window<T, NT>(a, ci, w, rb, rank, C);
         if (NBUF == 1) esync(C);

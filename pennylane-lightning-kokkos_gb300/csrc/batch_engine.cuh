@@ -434,4 +434,173 @@ __device__ __forceinline__ uint32_t diag_index(uint32_t idx, uint32_t bits, int 
     return g;
 }
 
+template <class T, bool BWD>
+__device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps], c2_t<T> (&hv)[kWinAmps], uint32_t base,
+                                          const uint32_t (&bb)[4], const c2_t<T> *__restrict__ mats, EAcc<T> &acc,
+                                          EAcc<T> &acc1) {
+    using V = c2_t<T>;
+    const bool tr = BWD && op.red != 0xff;
+    if (op.kind == EK_DENSE) {
+        const V *U = mats + op.mat;
+#define PLK_DENSE1_CASE(S_)                                                                                           \
+    case 16 + S_:                                                                                                      \
+        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
+        dense_apply<1, S_>(lv, U);                                                                                     \
+        if (BWD) dense_apply<1, S_>(hv, U);                                                                            \
+        break;                                                                                                         \
+    case 16 + 4 + S_:                                                                                                  \
+        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
+        rx_apply<S_>(lv, U);                                                                                           \
+        if (BWD) rx_apply<S_>(hv, U);                                                                                  \
+        break;                                                                                                         \
+    case 16 + 8 + S_:                                                                                                  \
+        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
+        ry_apply<S_>(lv, U);                                                                                           \
+        if (BWD) ry_apply<S_>(hv, U);                                                                                  \
+        break;
+#define PLK_DENSE_CASE(K_, S_)                                                                                        \
+    case K_ * 16 + S_:                                                                                                 \
+        if (tr) dense_gen_dot<K_, S_, T>(lv, hv, mats + op.gen, acc);                                                  \
+        dense_apply<K_, S_>(lv, U);                                                                                    \
+        if (BWD) dense_apply<K_, S_>(hv, U);                                                                           \
+        break;
+        switch (op.K * 16 + op.sel) {
+            PLK_DENSE1_CASE(0) PLK_DENSE1_CASE(1) PLK_DENSE1_CASE(2) PLK_DENSE1_CASE(3)
+            PLK_DENSE_CASE(2, 0) PLK_DENSE_CASE(2, 1) PLK_DENSE_CASE(2, 2) PLK_DENSE_CASE(2, 3)
+            PLK_DENSE_CASE(2, 4) PLK_DENSE_CASE(2, 5)
+        default: {
+            // K = 3, 4: sel = missing register bit (K = 3) or 0 (K = 4)
+            // (copies keep lv / hv themselves in registers)
+            const uint32_t smask = op.K == 4 ? 15u : (15u & ~(1u << op.sel));
+            V tl[kWinAmps], th[kWinAmps];
+#pragma unroll
+            for (int j = 0; j < kWinAmps; j++) {
+                tl[j] = lv[j];
+                th[j] = hv[j];
+            }
+            if (tr) dense_gen_dot_rt<T>(tl, th, mats + op.gen, op.K, smask, acc);
+            dense_apply_rt(tl, U, op.K, smask);
+            if (BWD) dense_apply_rt(th, U, op.K, smask);
+#pragma unroll
+            for (int j = 0; j < kWinAmps; j++) {
+                lv[j] = tl[j];
+                hv[j] = th[j];
+            }
+            break;
+        }
+        }
+#undef PLK_DENSE_CASE
+#undef PLK_DENSE1_CASE
+    } else if (op.kind == EK_CX) {
+#define PLK_CX_CASE(C_, T_)                                                                                           \
+    case C_ * 4 + T_:                                                                                                  \
+        cx_apply<C_, T_>(lv);                                                                                          \
+        if (BWD) cx_apply<C_, T_>(hv);                                                                                 \
+        break;
+        switch (op.sel) {
+            PLK_CX_CASE(0, 1) PLK_CX_CASE(0, 2) PLK_CX_CASE(0, 3) PLK_CX_CASE(1, 0) PLK_CX_CASE(1, 2)
+            PLK_CX_CASE(1, 3) PLK_CX_CASE(2, 0) PLK_CX_CASE(2, 1) PLK_CX_CASE(2, 3) PLK_CX_CASE(3, 0)
+            PLK_CX_CASE(3, 1) PLK_CX_CASE(3, 2)
+        default: break;
+        }
+#undef PLK_CX_CASE
+    } else if (op.kind == EK_DIAG && op.K == 1) {
+        // one-wire diagonal (RZ, PhaseShift, Z, S, T): two phases by one bit
+        const uint32_t b0 = op.bits & 31u;
+        const V e0 = mats[op.mat], e1 = mats[op.mat + 1];
+        T g0 = 0, g1 = 0;
+        if (tr) {
+            g0 = mats[op.gen].x;
+            g1 = mats[op.gen + 1].x;
+        }
+        T t = 0;
+#pragma unroll
+        for (int j = 0; j < kWinAmps; j++) {
+            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                 ((j & 8) ? bb[3] : 0);
+            const bool one = (idx >> b0) & 1u;
+            if (tr) {
+                // Im(conj(h) g v) = g (h.x v.y - h.y v.x); two amplitudes per FP32 partial
+                const T gd = one ? g1 : g0;
+                t = fma(gd * hv[j].x, lv[j].y, t);
+                t = fma(-gd * hv[j].y, lv[j].x, t);
+                if (j & 1) {
+                    ((j >> 1) & 1 ? acc1 : acc).addf(t);
+                    t = 0;
+                }
+            }
+            const V e = one ? e1 : e0;
+            lv[j] = cmul(lv[j], e);
+            if (BWD) hv[j] = cmul(hv[j], e);
+        }
+    } else {
+        const bool parity = op.kind == EK_PARITY;
+#pragma unroll
+        for (int j = 0; j < kWinAmps; j++) {
+            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                 ((j & 8) ? bb[3] : 0);
+            const uint32_t g = parity ? (uint32_t)(__popc(idx & op.bits) & 1) : diag_index(idx, op.bits, op.K);
+            const V e = mats[op.mat + g];
+            if (tr) {
+                // generator diagonal: MultiRZ (-1)^parity, otherwise real entries 0, +-1
+                const T gd = parity ? (g ? (T)-1 : (T)1) : mats[op.gen + g].x;
+                (j & 1 ? acc1 : acc).im_dot(hv[j], mk<V>(gd * lv[j].x, gd * lv[j].y));
+            }
+            lv[j] = cmul(lv[j], e);
+            if (BWD) hv[j] = cmul(hv[j], e);
+        }
+    }
+}
+
+// One window over the work items u = t0, t0 + tstep, ... of a state: load the
+// 16 amplitudes of lambda (and H lambda going backwards), apply the window's
+// ops in registers, store them back; trainable ops add their per-thread
+// inner-product partials to part[slot * NT + threadIdx.x].
+template <class T, int NT, int MODE, bool BWD>
+__device__ __noinline__ void run_window(const EOp *__restrict__ ops, const c2_t<T> *__restrict__ mats, const EWin &w,
+                                        int nq, c2_t<T> *lam, c2_t<T> *hl, uint32_t t0, uint32_t tstep,
+                                        typename EAcc<T>::Slot *part) {
+    using V = c2_t<T>;
+    const int lane = threadIdx.x & 31;
+    const uint32_t nu = 1u << (nq - kWinBits);
+    const uint32_t bb[4] = {1u << w.rb[0], 1u << w.rb[1], 1u << w.rb[2], 1u << w.rb[3]};
+    for (uint32_t u = t0; u - lane < nu; u += tstep) {
+        const bool act = u < nu;
+        uint32_t base = u;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t lo = base & (bb[i] - 1);
+            base = ((base ^ lo) << 1) | lo;
+        }
+        V lv[kWinAmps], hv[kWinAmps];
+#pragma unroll
+        for (int j = 0; j < kWinAmps; j++) {
+            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                 ((j & 8) ? bb[3] : 0);
+            lv[j] = act ? eld<T, MODE>(lam, idx) : mk<V>(0, 0);
+            if (BWD) hv[j] = act ? eld<T, MODE>(hl, idx) : mk<V>(0, 0);
+            else hv[j] = mk<V>(0, 0);
+        }
+        for (int k = 0; k < w.nops; k++) {
+            const EOp op = ops[w.op0 + k];
+            EAcc<T> acc, acc1;
+            if (BWD && op.red != 0xff) acc.load(part[op.red * NT + threadIdx.x]);
+            window_op<T, BWD>(op, lv, hv, base, bb, mats, acc, acc1);
+            if (BWD && op.red != 0xff) {
+                acc.merge(acc1);
+                part[op.red * NT + threadIdx.x] = acc.slot();
+            }
+        }
+        if (act) {
+#pragma unroll
+            for (int j = 0; j < kWinAmps; j++) {
+                const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                     ((j & 8) ? bb[3] : 0);
+                est<T, MODE>(lam, idx, lv[j]);
+                if (BWD) est<T, MODE>(hl, idx, hv[j]);
+            }
+        }
+    }
+}
+
 } // namespace plk

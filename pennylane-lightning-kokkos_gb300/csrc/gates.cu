@@ -89,6 +89,8 @@ static void set_extras_list(GatePlan &p, int mode, std::initializer_list<int> id
 }
 
 // Plan of a named gate (GateFunctors.hpp functor constructors).
+int window_apply_ops(plk_state s, const plk_op *ops, int nops, bool &handled);
+
 int plan_gate(int gate, int nw, bool inv, const double *prm, int np, GatePlan &p) {
     if (gate < 0 || gate >= PLK_GATE_COUNT || gate == PLK_GATE_MATRIX)
         PLK_FAIL(PLK_ERR_UNKNOWN_GATE, "unknown gate id " + std::to_string(gate));
@@ -704,6 +706,11 @@ PLK_API int plk_apply_ops(plk_state s, const plk_op *ops, int32_t nops) {
     PLK_TRY(check_state(s));
     if (nops > 0 && !ops) PLK_FAIL(PLK_ERR_INVALID_ARG, "null ops");
     PLK_CUDA(cudaSetDevice(s->device));
+    {
+        bool handled = false;
+        PLK_TRY(window_apply_ops(s, ops, nops, handled));
+        if (handled) return PLK_OK;
+    }
     for (int i = 0; i < nops; i++) {
         const plk_op &o = ops[i];
         int st = apply_gate_impl(s, o.gate, o.wires, o.num_wires, o.adjoint != 0, o.params, o.num_params, o.matrix);

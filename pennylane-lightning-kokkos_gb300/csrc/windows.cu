@@ -1,0 +1,297 @@
+// windows.cu — register-window sweeps over one large state.
+//
+// The op-at-a-time paths read and write the whole state once per gate.  Here
+// an op sequence is packed into 4-qubit register windows (the compiler of the
+// batch engine, window_host.cuh) and each window is one kernel over the
+// whole GPU: every thread loads the 16 amplitudes that differ in the window
+// bits, applies all of the window's ops in registers and stores them once.
+// A layer of RY, RZ on every wire plus a CNOT ladder needs about 0.6 state
+// passes per wire instead of 3.
+//
+// Used for complex64 states by
+//   plk_apply_ops           (StateVectorKokkos::applyOperation over a tape,
+//                            StateVectorKokkos.hpp:585-676), and
+//   plk_adjoint_jacobian    with one observable (AdjointDiffKokkos.hpp:404-478):
+//                            walking the ops backwards, each window applies
+//                            U^dag to lambda and H lambda and accumulates
+//                            -2 scale Im <H lambda | G lambda> per trainable op
+//                            (double-float accumulation; per-block partials
+//                            reduced in block order, so reruns are bitwise
+//                            identical).
+// Ops outside the window model (gates on more than four wires other than
+// MultiRZ; for the adjoint, ops with more than one parameter, which the
+// reference rejects) keep the op-at-a-time path.  plk_set_window_path(0)
+// turns the window path off.
+#include <atomic>
+#include <vector>
+
+#include "window_host.cuh"
+
+namespace plk {
+
+namespace {
+std::atomic<int> g_window_path{1};
+constexpr int kWinThreads = 256;
+} // namespace
+
+template <class T, bool BWD>
+__global__ void __launch_bounds__(kWinThreads, 2)
+    k_state_window(c2_t<T> *lam, c2_t<T> *hl, int nq, const EWin *__restrict__ wins, int wi,
+                   const EOp *__restrict__ ops, const c2_t<T> *__restrict__ mats, const ETrain *__restrict__ train,
+                   double *__restrict__ bpart) {
+    using Slot = typename EAcc<T>::Slot;
+    __shared__ Slot part[kMaxWinTrain * kWinThreads];
+    const EWin w = wins[wi];
+    if (BWD)
+        for (int t = 0; t < w.ntrain; t++) part[t * kWinThreads + threadIdx.x] = Slot{};
+    run_window<T, kWinThreads, EM_GLOBAL, BWD>(ops, mats, w, nq, lam, hl, blockIdx.x * kWinThreads + threadIdx.x,
+                                               gridDim.x * kWinThreads, part);
+    if (BWD && w.ntrain > 0) {
+        __syncthreads();
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        for (int t = warp; t < w.ntrain; t += kWinThreads / 32) {
+            EAcc<T> acc;
+#pragma unroll
+            for (int i = 0; i < kWinThreads / 32; i++) {
+                EAcc<T> x;
+                x.load(part[t * kWinThreads + i * 32 + lane]);
+                acc.merge(x);
+            }
+            const double s = acc.warp_sum();
+            if (lane == 0) {
+                const ETrain tr = train[w.tr0 + t];
+                bpart[(size_t)tr.slot * gridDim.x + blockIdx.x] = (double)tr.gscale * s;
+            }
+        }
+    }
+}
+
+// jac[s] = sum over blocks, in block order
+__global__ void k_window_jac(const double *__restrict__ bpart, int nblocks, int ntp, double *__restrict__ jac) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ntp) return;
+    double t = 0.0;
+    for (int b = 0; b < nblocks; b++) t += bpart[(size_t)s * nblocks + b];
+    jac[s] = t;
+}
+
+struct StateProgram {
+    std::vector<EWin> wins;
+    std::vector<EOp> ops;
+    std::vector<ETrain> train;
+    std::vector<EPrep> prep; // unused: matrices come from the ops themselves
+    std::vector<double2> gen;
+    std::vector<double2> mats;
+    int64_t n_mats = 0;
+};
+
+// XOp of a reference op with its matrix U_op (gate order); false if the op
+// does not fit the window model.
+static int make_xop(const plk_op &op, int nq, XOp &x, bool &fits) {
+    fits = true;
+    x = XOp();
+    x.gate = op.gate;
+    x.inv = op.adjoint != 0;
+    x.pidx = -1;
+    x.slot = -1;
+    x.basis = -1;
+    x.user_matrix = -1;
+    const int g = op.gate;
+    if (g == PLK_GATE_MULTIRZ) {
+        if (op.num_wires < 1 || op.num_wires > 32) {
+            fits = false;
+            return PLK_OK;
+        }
+        x.kind = EK_PARITY;
+        x.K = 1;
+        x.mrz_wires.assign(op.wires, op.wires + op.num_wires);
+        GatePlan p;
+        PLK_TRY(plan_gate(g, 1, x.inv, op.params, op.num_params, p));
+        plan_dense(p, 1, x.umat);
+        return PLK_OK;
+    }
+    if (op.num_wires > kWinBits || op.num_wires < 1) {
+        fits = false;
+        return PLK_OK;
+    }
+    x.K = op.num_wires;
+    for (int j = 0; j < x.K; j++) x.wires[j] = (int)op.wires[j];
+    if (g == PLK_GATE_MATRIX) {
+        if (!op.matrix) PLK_FAIL(PLK_ERR_INVALID_ARG, "matrix op without a matrix");
+        const int D = 1 << x.K;
+        x.umat.resize((size_t)D * D);
+        for (int r = 0; r < D; r++)
+            for (int c = 0; c < D; c++) {
+                // the op applies the matrix, or its conjugate transpose when adjoint
+                const int src = x.inv ? c * D + r : r * D + c;
+                x.umat[(size_t)r * D + c] = mk<double2>(op.matrix[2 * src], x.inv ? -op.matrix[2 * src + 1]
+                                                                                  : op.matrix[2 * src + 1]);
+            }
+        x.kind = EK_DENSE;
+        return PLK_OK;
+    }
+    GatePlan p;
+    PLK_TRY(plan_gate(g, op.num_wires, x.inv, op.params, op.num_params, p));
+    plan_dense(p, x.K, x.umat);
+    x.kind = g == PLK_GATE_CNOT ? EK_CX : (is_diag_gate(g) ? EK_DIAG : EK_DENSE);
+    return PLK_OK;
+}
+
+template <class T>
+static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool bwd, int ntp, double *jac_host) {
+    using V = c2_t<T>;
+    DeviceCtx *d = nullptr;
+    PLK_TRY(device_ctx(lam->device, &d));
+    cudaStream_t st = lam->stream;
+    const uint64_t nu = lam->length >> kWinBits;
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)d->sm_count * 2,
+                                                                    (nu + kWinThreads - 1) / kWinThreads));
+    std::vector<V> mats(P.mats.size() + P.gen.size());
+    for (size_t i = 0; i < P.mats.size(); i++) mats[i] = mk<V>((T)P.mats[i].x, (T)P.mats[i].y);
+    for (size_t i = 0; i < P.gen.size(); i++) mats[P.mats.size() + i] = mk<V>((T)P.gen[i].x, (T)P.gen[i].y);
+    std::vector<EOp> ops = P.ops;
+    for (auto &o : ops)
+        if (o.gen >= 0) o.gen += (int32_t)P.mats.size();
+    const size_t b_w = P.wins.size() * sizeof(EWin), b_o = ops.size() * sizeof(EOp);
+    const size_t b_t = std::max<size_t>(1, P.train.size()) * sizeof(ETrain), b_m = std::max<size_t>(1, mats.size()) * sizeof(V);
+    const size_t b_p = bwd ? (size_t)std::max(1, ntp) * grid * sizeof(double) : 0;
+    const size_t b_j = bwd ? (size_t)std::max(1, ntp) * sizeof(double) : 0;
+    auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const size_t total = al(b_w) + al(b_o) + al(b_t) + al(b_m) + al(b_p) + al(b_j);
+    char *buf = nullptr;
+    PLK_CUDA(cudaMallocAsync((void **)&buf, total, st));
+    char *p = buf;
+    EWin *d_w = (EWin *)p;
+    p += al(b_w);
+    EOp *d_o = (EOp *)p;
+    p += al(b_o);
+    ETrain *d_t = (ETrain *)p;
+    p += al(b_t);
+    V *d_m = (V *)p;
+    p += al(b_m);
+    double *d_p = (double *)p;
+    p += al(b_p);
+    double *d_j = (double *)p;
+    int rc = PLK_OK;
+    auto cp = [&](void *dst, const void *src, size_t n) {
+        if (rc == PLK_OK && n && cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, st) != cudaSuccess)
+            rc = PLK_ERR_CUDA;
+    };
+    cp(d_w, P.wins.data(), b_w);
+    cp(d_o, ops.data(), b_o);
+    if (!P.train.empty()) cp(d_t, P.train.data(), P.train.size() * sizeof(ETrain));
+    if (!mats.empty()) cp(d_m, mats.data(), mats.size() * sizeof(V));
+    if (bwd && rc == PLK_OK && cudaMemsetAsync(d_p, 0, b_p, st) != cudaSuccess) rc = PLK_ERR_CUDA;
+    V *lp = (V *)lam->data;
+    V *hp = hl ? (V *)hl->data : nullptr;
+    for (size_t wi = 0; wi < P.wins.size() && rc == PLK_OK; wi++) {
+        if (bwd)
+            k_state_window<T, true><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p);
+        else
+            k_state_window<T, false><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p);
+        if (cudaGetLastError() != cudaSuccess) rc = PLK_ERR_CUDA;
+    }
+    if (bwd && rc == PLK_OK && ntp > 0) {
+        k_window_jac<<<(ntp + 255) / 256, 256, 0, st>>>(d_p, grid, ntp, d_j);
+        if (cudaGetLastError() != cudaSuccess) rc = PLK_ERR_CUDA;
+        if (rc == PLK_OK &&
+            cudaMemcpyAsync(jac_host, d_j, ntp * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            rc = PLK_ERR_CUDA;
+    }
+    cudaFreeAsync(buf, st);
+    if (rc != PLK_OK) PLK_FAIL(rc, std::string("window sweep failed: ") + cudaGetErrorString(cudaGetLastError()));
+    if (bwd) PLK_CUDA(cudaStreamSynchronize(st));
+    return PLK_OK;
+}
+
+bool window_path_enabled() { return g_window_path.load() != 0; }
+
+// Forward: the whole op list through windows (complex64).
+int window_apply_ops(plk_state s, const plk_op *ops, int nops, bool &handled) {
+    handled = false;
+    if (!window_path_enabled() || s->dtype != PLK_C64 || nops < 4 || s->nq < 6 || s->nq > 32) return PLK_OK;
+    std::vector<XOp> xs;
+    xs.reserve(nops * 3);
+    for (int i = 0; i < nops; i++) {
+        const plk_op &op = ops[i];
+        if (op.gate < 0 || op.gate >= PLK_GATE_COUNT) return PLK_OK; // the per-op path reports it
+        if (op.gate == PLK_GATE_IDENTITY) continue;
+        if (check_wires(s, op.wires, op.num_wires) != PLK_OK) return PLK_OK;
+        if (op.num_params < plk_gate_num_params(op.gate) || (op.num_params > 0 && !op.params)) return PLK_OK;
+        XOp x;
+        bool fits = false;
+        if (make_xop(op, s->nq, x, fits) != PLK_OK) return PLK_OK;
+        if (!fits) return PLK_OK;
+        xs.push_back(std::move(x));
+    }
+    StateProgram P;
+    WinBuilder wb{s->nq, false, P.wins, P.ops, P.train, P.prep, P.gen, P.n_mats};
+    wb.hmats = &P.mats;
+    for (const auto &x : xs) PLK_TRY(wb.add(x));
+    PLK_TRY(wb.close());
+    handled = true;
+    return run_program<float>(s, nullptr, P, false, 0, nullptr);
+}
+
+// Backward sweep of the adjoint Jacobian with one observable (complex64);
+// `lam` is the working copy of the forward state (overwritten).
+int window_adjoint(plk_state lam, plk_state hl, const plk_op *ops, int nops, const int64_t *tp, int ntp, double *jac,
+                   bool &handled) {
+    handled = false;
+    if (!window_path_enabled() || lam->dtype != PLK_C64 || lam->nq < 6 || lam->nq > 32 || ntp <= 0) return PLK_OK;
+    int num_param_ops = 0;
+    for (int i = 0; i < nops; i++)
+        if (ops[i].num_params > 0) num_param_ops++;
+    // the reference's backward walk: ops in reverse until every trainable
+    // parameter is done (AdjointDiffKokkos.hpp:436-470)
+    std::vector<XOp> xs;
+    long current_param_idx = num_param_ops - 1;
+    int tp_it = ntp - 1;
+    for (int i = nops - 1; i >= 0 && tp_it >= 0; i--) {
+        const plk_op &op = ops[i];
+        if (op.num_params > 1) return PLK_OK; // rejected by the reference; the per-op path reports it
+        if (op.gate < 0 || op.gate >= PLK_GATE_COUNT) return PLK_OK;
+        const bool trainable = op.num_params > 0 && current_param_idx == tp[tp_it];
+        if (op.gate != PLK_GATE_IDENTITY) {
+            XOp x;
+            bool fits = false;
+            if (make_xop(op, lam->nq, x, fits) != PLK_OK || !fits) return PLK_OK;
+            if (trainable) {
+                GatePlan gp;
+                if (plan_generator(op.gate, op.num_wires, gp) != PLK_OK) return PLK_OK;
+                x.slot = tp_it;
+            }
+            xs.push_back(std::move(x));
+        } else if (trainable) {
+            return PLK_OK;
+        }
+        if (trainable) tp_it--;
+        if (op.num_params > 0) current_param_idx--;
+    }
+    StateProgram P;
+    WinBuilder wb{lam->nq, true, P.wins, P.ops, P.train, P.prep, P.gen, P.n_mats};
+    wb.hmats = &P.mats;
+    for (const auto &x : xs) PLK_TRY(wb.add(x));
+    PLK_TRY(wb.close());
+    handled = true;
+    std::vector<double> j(ntp, 0.0);
+    PLK_TRY(run_program<float>(lam, hl, P, true, ntp, j.data()));
+    for (int t = 0; t < ntp; t++) jac[t] = j[t];
+    return PLK_OK;
+}
+
+} // namespace plk
+
+extern "C" {
+
+PLK_API int plk_set_window_path(int32_t enable) {
+    plk::g_window_path.store(enable != 0);
+    return PLK_OK;
+}
+
+PLK_API int plk_get_window_path(int32_t *enabled) {
+    if (enabled) *enabled = plk::g_window_path.load();
+    return PLK_OK;
+}
+
+} // extern "C"

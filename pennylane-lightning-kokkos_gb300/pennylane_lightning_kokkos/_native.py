@@ -99,6 +99,8 @@ _SIGS = {
     "plk_adjoint_jacobian_inplace": ([_vp, C.POINTER(_vp), C.c_int32, C.POINTER(PlkOp), C.c_int32, _i64p, C.c_int32,
                                       _dp], C.c_int),
     "plk_expval_pauliz_noalloc": ([_vp, C.c_int32, C.c_int32, C.c_int32, _i64p, _dp, _vp], C.c_int),
+    "plk_set_window_path": ([C.c_int32], C.c_int),
+    "plk_get_window_path": ([_i32p], C.c_int),
     "plk_gate_matrix": ([C.c_int32, _dp, C.c_int32, C.c_int32, C.c_int32, _dp], C.c_int),
     "plk_batch_create": ([C.c_int32, C.c_int32, C.POINTER(_vp)], C.c_int),
     "plk_batch_destroy": ([_vp], C.c_int),

@@ -1,0 +1,154 @@
+"""GPU: register-window sweeps over one state (complex64 op lists and
+one-observable adjoint Jacobians) against the op-at-a-time path and the oracle.
+
+Tolerances: states within 5e-6 (complex64 rounding) of the op-at-a-time path
+and of the FP64 oracle; Jacobians within 1e-4 of the oracle and 2e-5 of the
+op-at-a-time complex64 path; window results are bitwise reproducible.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+from abi import State, i64, make_ops
+from pennylane_lightning_kokkos import _native as N
+from test_gpu_adjoint import gpu_adjoint, random_circuit
+from test_oracle_golden import ALL_GATES
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def window_switch():
+    old = C.c_int32()
+    N.check(N.lib.plk_get_window_path(C.byref(old)))
+    yield lambda on: N.check(N.lib.plk_set_window_path(int(on)))
+    N.check(N.lib.plk_set_window_path(old.value))
+
+
+def run_forward(nq, ops, dtype=N.PLK_C64):
+    s = State(nq, dtype)
+    arr, keep = make_ops(ops)
+    N.check(N.lib.plk_apply_ops(s.h, arr, len(ops)))
+    out = s.get()
+    s.close()
+    return out
+
+
+def circuit_with_everything(nq, nops, rng):
+    from pennylane_lightning_kokkos.circuits import haar_unitary
+
+    ops = []
+    for _ in range(nops):
+        r = rng.random()
+        if r < 0.1:
+            k = int(rng.integers(1, 5))
+            ops.append(("Matrix", [int(w) for w in rng.choice(nq, k, replace=False)], bool(rng.integers(2)), [],
+                        haar_unitary(1 << k, rng)))
+        elif r < 0.2:
+            k = int(rng.integers(1, nq + 1))
+            ops.append(("MultiRZ", [int(w) for w in rng.choice(nq, k, replace=False)], bool(rng.integers(2)),
+                        [float(rng.uniform(0, 6))]))
+        else:
+            name = str(rng.choice(sorted(ALL_GATES)))
+            nw, npar = ALL_GATES[name]
+            if nw < 0:
+                continue
+            ops.append((name, [int(w) for w in rng.choice(nq, nw, replace=False)], bool(rng.integers(2)),
+                        list(rng.uniform(0, 2 * np.pi, npar))))
+    return ops
+
+
+def oracle_forward(nq, ops):
+    psi = O.zero_state(nq)
+    for op in ops:
+        if op[0] == "Matrix":
+            O.apply_matrix(psi, op[4], op[1], op[2])
+        else:
+            O.apply(psi, op[0], op[1], op[2], op[3])
+    return psi
+
+
+@pytest.mark.parametrize("nq", [6, 9, 12])
+def test_window_forward_matches_per_op_and_oracle(nq, window_switch):
+    rng = np.random.default_rng(100 + nq)
+    ops = circuit_with_everything(nq, 120, rng)
+    window_switch(True)
+    a = run_forward(nq, ops)
+    b = run_forward(nq, ops)
+    window_switch(False)
+    c = run_forward(nq, ops)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_allclose(a, c, atol=5e-6, rtol=0)
+    np.testing.assert_allclose(a, oracle_forward(nq, ops), atol=5e-6, rtol=0)
+
+
+def test_window_forward_layered_ansatz(window_switch):
+    from pennylane_lightning_kokkos.circuits import hardware_efficient_ansatz
+
+    nq = 14
+    ops = hardware_efficient_ansatz(nq, 6, seed=9, rotations=("RX", "RY", "RZ"))
+    window_switch(True)
+    a = run_forward(nq, ops)
+    np.testing.assert_allclose(a, O.run_ops(O.zero_state(nq), ops), atol=5e-6, rtol=0)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_window_adjoint_matches_oracle(seed, window_switch):
+    rng = np.random.default_rng(seed)
+    nq = 8 + seed
+    ops = random_circuit(nq, 80, rng)
+    npar = sum(1 for o in ops if o[3])
+    trainable = sorted(int(x) for x in rng.choice(npar, max(1, npar * 2 // 3), replace=False))
+    obs = [("hamiltonian", [0.7, -0.4, 1.1],
+            [("named", "PauliZ", [1]), ("tensor", [("named", "PauliX", [0]), ("named", "PauliY", [3])]),
+             ("named", "PauliX", [nq - 1])])]
+    psi = O.run_ops(O.zero_state(nq), ops)
+    ref = O.adjoint_jacobian(psi, obs, ops, trainable)
+    window_switch(True)
+    jw = gpu_adjoint(psi, obs, ops, trainable, N.PLK_C64)
+    jw2 = gpu_adjoint(psi, obs, ops, trainable, N.PLK_C64)
+    window_switch(False)
+    jp = gpu_adjoint(psi, obs, ops, trainable, N.PLK_C64)
+    np.testing.assert_array_equal(jw, jw2)
+    np.testing.assert_allclose(jw, ref, atol=1e-4, rtol=0)
+    np.testing.assert_allclose(jw, jp, atol=2e-5, rtol=0)
+
+
+def test_window_adjoint_matrices_and_multirz(window_switch):
+    """Non-trainable matrix ops and trainable MultiRZ on many wires."""
+    from pennylane_lightning_kokkos.circuits import haar_unitary
+
+    rng = np.random.default_rng(5)
+    nq = 10
+    ops = []
+    for k in range(30):
+        if k % 7 == 3:
+            kk = int(rng.integers(1, 5))
+            ops.append(("Matrix", [int(w) for w in rng.choice(nq, kk, replace=False)], bool(rng.integers(2)), [],
+                        haar_unitary(1 << kk, rng)))
+        elif k % 5 == 0:
+            ops.append(("MultiRZ", [int(w) for w in rng.choice(nq, 6, replace=False)], bool(rng.integers(2)),
+                        [float(rng.uniform(0, 6))]))
+        else:
+            ops.append(("RY", [k % nq], False, [float(rng.uniform(0, 6))]))
+            ops.append(("CNOT", [k % nq, (k + 3) % nq], False, []))
+    npar = sum(1 for o in ops if o[3])
+    psi = oracle_forward(nq, ops)
+    obs = [("named", "PauliZ", [2])]
+    window_switch(False)
+    jp128 = gpu_adjoint(psi, obs, ops, list(range(npar)), N.PLK_C128)
+    window_switch(True)
+    jw = gpu_adjoint(psi, obs, ops, list(range(npar)), N.PLK_C64)
+    np.testing.assert_allclose(jw, jp128, atol=1e-4, rtol=0)
+
+
+def test_window_switch_roundtrip(window_switch):
+    v = C.c_int32()
+    window_switch(False)
+    N.check(N.lib.plk_get_window_path(C.byref(v)))
+    assert v.value == 0
+    window_switch(True)
+    N.check(N.lib.plk_get_window_path(C.byref(v)))
+    assert v.value == 1

@@ -262,3 +262,25 @@ def test_adjoint_matches_central_differences():
             vals.append(O.expval_observable(O.run_ops(O.zero_state(nq), ops2), ham))
         assert jac[k] == pytest.approx((vals[0] - vals[1]) / (2 * h), abs=1e-7)
         k += 1
+
+
+def test_multirz_on_many_wires_matches_formula():
+    """MultiRZ acts on any number of wires: exp(-i theta/2 Z...Z), a phase by
+    the parity of the selected bits (multiRZFunctor, GateFunctors.hpp:2132-2170)."""
+    rng = np.random.default_rng(7)
+    for nq in (9, 12, 14):
+        for k in (1, 5, nq):
+            wires = [int(w) for w in rng.permutation(nq)[:k]]
+            th = float(rng.uniform(-3, 3))
+            psi = rng.normal(size=1 << nq) + 1j * rng.normal(size=1 << nq)
+            mask = sum(1 << (nq - 1 - w) for w in wires)
+            par = np.array([bin(i & mask).count("1") & 1 for i in range(1 << nq)])
+            for inv in (False, True):
+                ph = np.where(par, np.exp(1j * th / 2), np.exp(-1j * th / 2))
+                ref = psi * (np.conj(ph) if inv else ph)
+                out = psi.copy()
+                O.apply(out, "MultiRZ", wires, inv, [th])
+                np.testing.assert_allclose(out, ref, atol=1e-14)
+                g = psi.copy()
+                O.apply_generator(g, "MultiRZ", wires)
+                np.testing.assert_allclose(g, psi * np.where(par, -1.0, 1.0), atol=1e-15)
