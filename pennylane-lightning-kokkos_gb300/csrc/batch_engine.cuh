@@ -356,9 +356,9 @@ __device__ __forceinline__ void dense_gen_dot(const V (&v)[kWinAmps], const V (&
 
 // acc += Im <h | G v> for a one-wire generator on register bit Q given as a
 // monomial pattern (see EOp::bits): row r takes i^q v[col] or nothing.  The
-// contribution of one amplitude pair (at most four products) is formed in the
-// state precision, then accumulated (double-float for complex64); even groups
-// go to a0, odd ones to a1 (two independent chains).
+// contribution of two amplitude pairs (at most eight products) is formed in
+// the state precision, then accumulated (double-float for complex64),
+// alternately into a0 and a1 (two independent chains).
 template <int Q, class T, class V>
 __device__ __forceinline__ void gen1_dot(const V (&v)[kWinAmps], const V (&h)[kWinAmps], uint32_t pat, EAcc<T> &a0,
                                          EAcc<T> &a1) {
@@ -377,10 +377,10 @@ __device__ __forceinline__ void gen1_dot(const V (&v)[kWinAmps], const V (&h)[kW
         sb[r] = on[r] ? (odd[r] ? sg : -sg) : (T)0;
     }
     int g = 0;
+    T t = 0;
 #pragma unroll
     for (int j = 0; j < kWinAmps; j++) {
         if (j & (1 << Q)) continue;
-        T t = 0;
 #pragma unroll
         for (int r = 0; r < 2; r++) {
             const V x = col[r] ? v[j | (1 << Q)] : v[j];
@@ -389,7 +389,68 @@ __device__ __forceinline__ void gen1_dot(const V (&v)[kWinAmps], const V (&h)[kW
             t = fma(sa[r] * hh.x, odd[r] ? x.x : x.y, t);
             t = fma(sb[r] * hh.y, odd[r] ? x.y : x.x, t);
         }
-        ((g++ & 1) ? a1 : a0).addf(t);
+        // two pairs (four amplitudes) per partial
+        if (g & 1) {
+            ((g >> 1) & 1 ? a1 : a0).addf(t);
+            t = 0;
+        }
+        g++;
+    }
+}
+
+// The same for the generators of RX (Pauli X) and RY (Pauli Y), with the
+// pattern known at compile time:
+//   X: Im(conj(h0) v1) + Im(conj(h1) v0)
+//   Y: Im(conj(h0) (-i v1)) + Im(conj(h1) (i v0)) = -Re(conj(h0) v1) + Re(conj(h1) v0)
+template <int Q, bool ISY, class T, class V>
+__device__ __forceinline__ void gen1_fixed(const V (&v)[kWinAmps], const V (&h)[kWinAmps], EAcc<T> &a0, EAcc<T> &a1) {
+    int g = 0;
+    T t = 0;
+#pragma unroll
+    for (int j = 0; j < kWinAmps; j++) {
+        if (j & (1 << Q)) continue;
+        const V v0 = v[j], v1 = v[j | (1 << Q)], h0 = h[j], h1 = h[j | (1 << Q)];
+        if (ISY) {
+            t = fma(-h0.x, v1.x, t);
+            t = fma(-h0.y, v1.y, t);
+            t = fma(h1.x, v0.x, t);
+            t = fma(h1.y, v0.y, t);
+        } else {
+            t = fma(h0.x, v1.y, t);
+            t = fma(-h0.y, v1.x, t);
+            t = fma(h1.x, v0.y, t);
+            t = fma(-h1.y, v0.x, t);
+        }
+        if (g & 1) {
+            ((g >> 1) & 1 ? a1 : a0).addf(t);
+            t = 0;
+        }
+        g++;
+    }
+}
+
+// One-wire diagonal on register bit Q: the phase (and generator entry) of
+// every register amplitude is known at compile time.  Generator partials are
+// formed over four amplitudes, then accumulated.
+template <int Q, class T, bool BWD, class V>
+__device__ __forceinline__ void diag1_reg(V (&lv)[kWinAmps], V (&hv)[kWinAmps], V e0, V e1, T g0, T g1, bool tr,
+                                          EAcc<T> &a0, EAcc<T> &a1) {
+    T t = 0;
+#pragma unroll
+    for (int j = 0; j < kWinAmps; j++) {
+        const bool one = (j >> Q) & 1;
+        if (tr) {
+            const T gd = one ? g1 : g0;
+            t = fma(gd * hv[j].x, lv[j].y, t);
+            t = fma(-gd * hv[j].y, lv[j].x, t);
+            if ((j & 3) == 3) {
+                ((j >> 2) & 1 ? a1 : a0).addf(t);
+                t = 0;
+            }
+        }
+        const V e = one ? e1 : e0;
+        lv[j] = cmul(lv[j], e);
+        if (BWD) hv[j] = cmul(hv[j], e);
     }
 }
 
@@ -449,12 +510,12 @@ __device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps]
         if (BWD) dense_apply<1, S_>(hv, U);                                                                            \
         break;                                                                                                         \
     case 16 + 4 + S_:                                                                                                  \
-        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
+        if (tr) gen1_fixed<S_, false, T>(lv, hv, acc, acc1);                                                           \
         rx_apply<S_>(lv, U);                                                                                           \
         if (BWD) rx_apply<S_>(hv, U);                                                                                  \
         break;                                                                                                         \
     case 16 + 8 + S_:                                                                                                  \
-        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
+        if (tr) gen1_fixed<S_, true, T>(lv, hv, acc, acc1);                                                            \
         ry_apply<S_>(lv, U);                                                                                           \
         if (BWD) ry_apply<S_>(hv, U);                                                                                  \
         break;
@@ -506,32 +567,37 @@ __device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps]
 #undef PLK_CX_CASE
     } else if (op.kind == EK_DIAG && op.K == 1) {
         // one-wire diagonal (RZ, PhaseShift, Z, S, T): two phases by one bit
-        const uint32_t b0 = op.bits & 31u;
         const V e0 = mats[op.mat], e1 = mats[op.mat + 1];
         T g0 = 0, g1 = 0;
         if (tr) {
             g0 = mats[op.gen].x;
             g1 = mats[op.gen + 1].x;
         }
-        T t = 0;
-#pragma unroll
-        for (int j = 0; j < kWinAmps; j++) {
-            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
-                                 ((j & 8) ? bb[3] : 0);
-            const bool one = (idx >> b0) & 1u;
-            if (tr) {
-                // Im(conj(h) g v) = g (h.x v.y - h.y v.x); two amplitudes per FP32 partial
-                const T gd = one ? g1 : g0;
-                t = fma(gd * hv[j].x, lv[j].y, t);
-                t = fma(-gd * hv[j].y, lv[j].x, t);
-                if (j & 1) {
-                    ((j >> 1) & 1 ? acc1 : acc).addf(t);
-                    t = 0;
-                }
-            }
+        switch (op.sel) {
+        case 0: diag1_reg<0, T, BWD>(lv, hv, e0, e1, g0, g1, tr, acc, acc1); break;
+        case 1: diag1_reg<1, T, BWD>(lv, hv, e0, e1, g0, g1, tr, acc, acc1); break;
+        case 2: diag1_reg<2, T, BWD>(lv, hv, e0, e1, g0, g1, tr, acc, acc1); break;
+        case 3: diag1_reg<3, T, BWD>(lv, hv, e0, e1, g0, g1, tr, acc, acc1); break;
+        default: {
+            // the bit is one of the thread's fixed bits: one phase for all 16 amplitudes
+            const bool one = (base >> (op.bits & 31u)) & 1u;
             const V e = one ? e1 : e0;
-            lv[j] = cmul(lv[j], e);
-            if (BWD) hv[j] = cmul(hv[j], e);
+            const T gd = one ? g1 : g0;
+            T t = 0;
+#pragma unroll
+            for (int j = 0; j < kWinAmps; j++) {
+                if (tr) {
+                    t = fma(gd * hv[j].x, lv[j].y, t);
+                    t = fma(-gd * hv[j].y, lv[j].x, t);
+                    if ((j & 3) == 3) {
+                        ((j >> 2) & 1 ? acc1 : acc).addf(t);
+                        t = 0;
+                    }
+                }
+                lv[j] = cmul(lv[j], e);
+                if (BWD) hv[j] = cmul(hv[j], e);
+            }
+        }
         }
     } else {
         const bool parity = op.kind == EK_PARITY;

@@ -342,32 +342,67 @@ struct PauliPass {
     int accumulate;
 };
 
+// out[m] (+)= sum over groups g of f_g(src) in[src], src = m ^ x_g, with
+// f_g(src) = sum_t c_t i^ny_t (-1)^popc(src & z_t).  complex64 states in FP32
+// (the result is stored in FP32); complex128 on the FP32 pipe in
+// double-float, rounded once to FP64.
 template <class T>
 __global__ void __launch_bounds__(kThreads)
     k_apply_pauli(c2_t<T> *__restrict__ out, const c2_t<T> *__restrict__ in, uint64_t n,
                   const PauliTerm *__restrict__ terms, const PauliPass pass) {
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t m = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; m < n; m += step) {
-        double ar = 0, ai = 0;
-        if (pass.accumulate) {
-            const c2_t<T> o = out[m];
-            ar = o.x;
-            ai = o.y;
-        }
-        for (int gi = 0; gi < pass.ngroups; gi++) {
-            const uint64_t src = m ^ pass.x[gi];
-            const c2_t<T> v = in[src];
-            double fr = 0, fi = 0;
-            for (int t = pass.first[gi]; t < pass.first[gi] + pass.count[gi]; t++) {
-                const PauliTerm tt = terms[t];
-                const double sg = (__popcll(src & tt.z) & 1) ? -1.0 : 1.0;
-                fr += sg * tt.cr;
-                fi += sg * tt.ci;
+        if constexpr (sizeof(T) == 4) {
+            float ar = 0.0f, ai = 0.0f;
+            if (pass.accumulate) {
+                const float2 o = out[m];
+                ar = o.x;
+                ai = o.y;
             }
-            ar += fr * v.x - fi * v.y;
-            ai += fr * v.y + fi * v.x;
+            for (int gi = 0; gi < pass.ngroups; gi++) {
+                const uint64_t src = m ^ pass.x[gi];
+                const float2 v = in[src];
+                float fr = 0.0f, fi = 0.0f;
+                for (int t = pass.first[gi]; t < pass.first[gi] + pass.count[gi]; t++) {
+                    const PauliTerm tt = terms[t];
+                    const bool neg = __popcll(src & tt.z) & 1;
+                    fr += neg ? -tt.crh : tt.crh;
+                    fi += neg ? -tt.cih : tt.cih;
+                }
+                ar = fmaf(fr, v.x, fmaf(-fi, v.y, ar));
+                ai = fmaf(fr, v.y, fmaf(fi, v.x, ai));
+            }
+            out[m] = make_float2(ar, ai);
+        } else {
+            DAcc ar, ai;
+            if (pass.accumulate) {
+                const CDF o = to_cdf(out[m]);
+                ar.add(o.re);
+                ai.add(o.im);
+            }
+            for (int gi = 0; gi < pass.ngroups; gi++) {
+                const uint64_t src = m ^ pass.x[gi];
+                const CDF v = to_cdf(in[src]);
+                DAcc fr, fi;
+                for (int t = pass.first[gi]; t < pass.first[gi] + pass.count[gi]; t++) {
+                    const PauliTerm tt = terms[t];
+                    const bool neg = __popcll(src & tt.z) & 1;
+                    if (neg) {
+                        fr.sub(DF{tt.crh, tt.crl});
+                        fi.sub(DF{tt.cih, tt.cil});
+                    } else {
+                        fr.add(DF{tt.crh, tt.crl});
+                        fi.add(DF{tt.cih, tt.cil});
+                    }
+                }
+                const DF f_re = fr.normalized(), f_im = fi.normalized();
+                ar.mac(f_re, v.re);
+                ar.msub(f_im, v.im);
+                ai.mac(f_re, v.im);
+                ai.mac(f_im, v.re);
+            }
+            out[m] = make_double2(ar.value(), ai.value());
         }
-        out[m] = mk<c2_t<T>>((T)ar, (T)ai);
     }
 }
 

@@ -299,6 +299,9 @@ struct WinBuilder {
                 uint32_t bits = 0;
                 for (int j = 0; j < o.K; j++) bits |= (uint32_t)(nq - 1 - o.wires[j]) << (5 * j);
                 e.bits = bits;
+                // one wire: its register bit (0..3), or 4 when the bit is fixed per thread
+                const int b0 = nq - 1 - o.wires[0];
+                e.sel = (uint8_t)(o.K == 1 && ((w >> b0) & 1u) ? pos[b0] : 4);
             } else { // parity
                 uint32_t mask = 0;
                 for (int wv : o.mrz_wires) mask |= 1u << (nq - 1 - wv);
