@@ -77,6 +77,9 @@ def parse_args(argv=None):
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--no-plain20", action="store_true")
+    ap.add_argument("--only", choices=["adjoint", "batch", "plain20", "precision"], default=None,
+                    help="run one secondary config alone and print its JSON (profiling and spot checks)")
+    ap.add_argument("--no-tune", action="store_true", help="batch: fixed launch configuration instead of autotuning")
     ap.add_argument("--precision", action="store_true",
                     help="also run the equal-bytes precision config (32-qubit complex64 vs 31-qubit complex128)")
     return ap.parse_args(argv)
@@ -469,14 +472,18 @@ def run_batch(args, device, torch):
     work = np.array([len(pk["gates"]) * float(1 << nq) for nq, pk, _ in wl])
     gate_apps = sum(len(pk["gates"]) for _, pk, _ in wl)
     # autotune on a one-in-sixteen subsample, then run the whole batch with the winner
-    sub = CircuitBatch("c64", device)
-    for nq, pk, words in wl[::16]:
-        sub.add_packed(nq, pk, words)
-    t = time.perf_counter()
-    report = sub.tune(reps=1)
-    tune_s = time.perf_counter() - t
-    cfg = sub.get_config()
-    sub.close()
+    if args.no_tune:
+        report, tune_s = "not tuned", 0.0
+        cfg = {"cluster": 8, "smem_qubits": 12, "cluster_min_qubits": 13, "ctas_per_sm": 2}
+    else:
+        sub = CircuitBatch("c64", device)
+        for nq, pk, words in wl[::16]:
+            sub.add_packed(nq, pk, words)
+        t = time.perf_counter()
+        report = sub.tune(reps=1)
+        tune_s = time.perf_counter() - t
+        cfg = sub.get_config()
+        sub.close()
     b = CircuitBatch("c64", device)
     for nq, pk, words in wl:
         b.add_packed(nq, pk, words)
@@ -713,6 +720,11 @@ def main(argv=None):
 
     device = local_rank
     torch.cuda.set_device(device)
+    if args.only:
+        if rank == 0:
+            fn = {"adjoint": run_adjoint, "batch": run_batch, "plain20": run_plain20, "precision": run_precision}
+            print(json.dumps({args.only: fn[args.only](args, device, torch)}), flush=True)
+        return 0
     dist = None
     if world > 1:
         import torch.distributed as dist
