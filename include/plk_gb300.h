@@ -244,9 +244,10 @@ PLK_API int plk_expval_pauliz_noalloc(const void *state, int32_t num_qubits, int
                                       const int64_t *wires, double *out, void *cuda_stream);
 
 /* ---- register-window path ----------------------------------------------- */
-/* complex64 op lists (plk_apply_ops) and one-observable adjoint Jacobians run
- * as register-window sweeps (about seven ops per state pass) unless this is
- * switched off; results agree with the op-at-a-time path to rounding. */
+/* Op lists (plk_apply_ops) and one-observable adjoint Jacobians run as
+ * register-window sweeps (about seven ops per state pass; complex128 in
+ * double-float on the FP32 pipe) unless this is switched off; results agree
+ * with the op-at-a-time path to rounding. */
 PLK_API int plk_set_window_path(int32_t enable);
 PLK_API int plk_get_window_path(int32_t *enabled);
 

@@ -495,13 +495,37 @@ __device__ __forceinline__ uint32_t diag_index(uint32_t idx, uint32_t bits, int 
     return g;
 }
 
-template <class T, bool BWD>
+// SLIM: only one-wire dense ops, one-wire diagonals and CNOTs (host-checked)
+template <class T, bool BWD, bool SLIM = false>
 __device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps], c2_t<T> (&hv)[kWinAmps], uint32_t base,
                                           const uint32_t (&bb)[4], const c2_t<T> *__restrict__ mats, EAcc<T> &acc,
                                           EAcc<T> &acc1) {
     using V = c2_t<T>;
     const bool tr = BWD && op.red != 0xff;
-    if (op.kind == EK_DENSE) {
+    if (SLIM && op.kind == EK_DENSE) {
+        const V *U = mats + op.mat;
+#define PLK_S1_CASE(S_)                                                                                               \
+    case S_:                                                                                                           \
+        if (tr) gen1_dot<S_, T>(lv, hv, op.bits, acc, acc1);                                                           \
+        dense_apply<1, S_>(lv, U);                                                                                     \
+        if (BWD) dense_apply<1, S_>(hv, U);                                                                            \
+        break;                                                                                                         \
+    case 4 + S_:                                                                                                       \
+        if (tr) gen1_fixed<S_, false, T>(lv, hv, acc, acc1);                                                           \
+        rx_apply<S_>(lv, U);                                                                                           \
+        if (BWD) rx_apply<S_>(hv, U);                                                                                  \
+        break;                                                                                                         \
+    case 8 + S_:                                                                                                       \
+        if (tr) gen1_fixed<S_, true, T>(lv, hv, acc, acc1);                                                            \
+        ry_apply<S_>(lv, U);                                                                                           \
+        if (BWD) ry_apply<S_>(hv, U);                                                                                  \
+        break;
+        switch (op.sel) {
+            PLK_S1_CASE(0) PLK_S1_CASE(1) PLK_S1_CASE(2) PLK_S1_CASE(3)
+        default: break;
+        }
+#undef PLK_S1_CASE
+    } else if (!SLIM && op.kind == EK_DENSE) {
         const V *U = mats + op.mat;
 #define PLK_DENSE1_CASE(S_)                                                                                           \
     case 16 + S_:                                                                                                      \
@@ -599,7 +623,7 @@ __device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps]
             }
         }
         }
-    } else {
+    } else if (!SLIM) {
         const bool parity = op.kind == EK_PARITY;
 #pragma unroll
         for (int j = 0; j < kWinAmps; j++) {
@@ -622,7 +646,7 @@ __device__ __forceinline__ void window_op(const EOp &op, c2_t<T> (&lv)[kWinAmps]
 // 16 amplitudes of lambda (and H lambda going backwards), apply the window's
 // ops in registers, store them back; trainable ops add their per-thread
 // inner-product partials to part[slot * NT + threadIdx.x].
-template <class T, int NT, int MODE, bool BWD>
+template <class T, int NT, int MODE, bool BWD, bool SLIM = false>
 __device__ __noinline__ void run_window(const EOp *__restrict__ ops, const c2_t<T> *__restrict__ mats, const EWin &w,
                                         int nq, c2_t<T> *lam, c2_t<T> *hl, uint32_t t0, uint32_t tstep,
                                         typename EAcc<T>::Slot *part) {
@@ -651,7 +675,7 @@ __device__ __noinline__ void run_window(const EOp *__restrict__ ops, const c2_t<
             const EOp op = ops[w.op0 + k];
             EAcc<T> acc, acc1;
             if (BWD && op.red != 0xff) acc.load(part[op.red * NT + threadIdx.x]);
-            window_op<T, BWD>(op, lv, hv, base, bb, mats, acc, acc1);
+            window_op<T, BWD, SLIM>(op, lv, hv, base, bb, mats, acc, acc1);
             if (BWD && op.red != 0xff) {
                 acc.merge(acc1);
                 part[op.red * NT + threadIdx.x] = acc.slot();

@@ -8,7 +8,8 @@
 // A layer of RY, RZ on every wire plus a CNOT ladder needs about 0.6 state
 // passes per wire instead of 3.
 //
-// Used for complex64 states by
+// Used (complex64; complex128 in double-float on the FP32 pipe, window_df.cuh,
+// unless PLK_C128_ARITH=fp64) by
 //   plk_apply_ops           (StateVectorKokkos::applyOperation over a tape,
 //                            StateVectorKokkos.hpp:585-676), and
 //   plk_adjoint_jacobian    with one observable (AdjointDiffKokkos.hpp:404-478):
@@ -25,6 +26,9 @@
 #include <atomic>
 #include <vector>
 
+#include <type_traits>
+
+#include "window_df.cuh"
 #include "window_host.cuh"
 
 namespace plk {
@@ -34,7 +38,7 @@ std::atomic<int> g_window_path{1};
 constexpr int kWinThreads = 256;
 } // namespace
 
-template <class T, bool BWD>
+template <class T, bool BWD, bool SLIM>
 __global__ void __launch_bounds__(kWinThreads, 2)
     k_state_window(c2_t<T> *lam, c2_t<T> *hl, int nq, const EWin *__restrict__ wins, int wi,
                    const EOp *__restrict__ ops, const c2_t<T> *__restrict__ mats, const ETrain *__restrict__ train,
@@ -44,7 +48,7 @@ __global__ void __launch_bounds__(kWinThreads, 2)
     const EWin w = wins[wi];
     if (BWD)
         for (int t = 0; t < w.ntrain; t++) part[t * kWinThreads + threadIdx.x] = Slot{};
-    run_window<T, kWinThreads, EM_GLOBAL, BWD>(ops, mats, w, nq, lam, hl, blockIdx.x * kWinThreads + threadIdx.x,
+    run_window<T, kWinThreads, EM_GLOBAL, BWD, SLIM>(ops, mats, w, nq, lam, hl, blockIdx.x * kWinThreads + threadIdx.x,
                                                gridDim.x * kWinThreads, part);
     if (BWD && w.ntrain > 0) {
         __syncthreads();
@@ -61,6 +65,99 @@ __global__ void __launch_bounds__(kWinThreads, 2)
             if (lane == 0) {
                 const ETrain tr = train[w.tr0 + t];
                 bpart[(size_t)tr.slot * gridDim.x + blockIdx.x] = (double)tr.gscale * s;
+            }
+        }
+    }
+}
+
+// complex128 windows on the FP32 pipe (window_df.cuh).  Between windows of
+// one sweep the states stay in double-float form in their own buffers (a
+// {re.hi, re.lo, im.hi, im.lo} float4 has the size of a double2): the first
+// window splits the doubles (in_df = 0), the last joins them back
+// (out_df = 0), the ones between move raw pairs.
+template <bool BWD, bool SLIM>
+__global__ void __launch_bounds__(kWinThreads, 1)
+    k_state_window_df(double2 *lam, double2 *hl, int nq, const EWin *__restrict__ wins, int wi,
+                      const EOp *__restrict__ ops, const float4 *__restrict__ mats, const ETrain *__restrict__ train,
+                      double *__restrict__ bpart, int in_df, int out_df) {
+    __shared__ float2 part[kMaxWinTrain * kWinThreads];
+    const EWin w = wins[wi];
+    const int tid = threadIdx.x;
+    if (BWD)
+        for (int t = 0; t < w.ntrain; t++) part[t * kWinThreads + tid] = make_float2(0.0f, 0.0f);
+    const uint32_t nu = 1u << (nq - kWinBits);
+    const uint32_t bb[4] = {1u << w.rb[0], 1u << w.rb[1], 1u << w.rb[2], 1u << w.rb[3]};
+    const uint32_t tstep = gridDim.x * kWinThreads;
+    for (uint32_t u = blockIdx.x * kWinThreads + tid; u < nu; u += tstep) {
+        uint32_t base = u;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t lo = base & (bb[i] - 1);
+            base = ((base ^ lo) << 1) | lo;
+        }
+        CDF lv[kWinAmps], hv[kWinAmps];
+#pragma unroll
+        for (int j = 0; j < kWinAmps; j++) {
+            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                 ((j & 8) ? bb[3] : 0);
+            if (in_df) {
+                const float4 a = reinterpret_cast<const float4 *>(lam)[idx];
+                lv[j] = {{a.x, a.y}, {a.z, a.w}};
+                if (BWD) {
+                    const float4 b = reinterpret_cast<const float4 *>(hl)[idx];
+                    hv[j] = {{b.x, b.y}, {b.z, b.w}};
+                } else {
+                    hv[j] = cdf_zero();
+                }
+            } else {
+                lv[j] = cdf_split(lam[idx]);
+                hv[j] = BWD ? cdf_split(hl[idx]) : cdf_zero();
+            }
+        }
+        for (int k = 0; k < w.nops; k++) {
+            const EOp op = ops[w.op0 + k];
+            DAcc acc, acc1;
+            if (BWD && op.red != 0xff) {
+                const float2 p = part[op.red * kWinThreads + tid];
+                acc.h = p.x;
+                acc.l = p.y;
+            }
+            window_op_df<BWD, SLIM>(op, lv, hv, base, bb, mats, acc, acc1);
+            if (BWD && op.red != 0xff) {
+                df_add(acc1.h, acc1.l, acc.h, acc.l);
+                part[op.red * kWinThreads + tid] = make_float2(acc.h, acc.l);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < kWinAmps; j++) {
+            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                 ((j & 8) ? bb[3] : 0);
+            if (out_df) {
+                reinterpret_cast<float4 *>(lam)[idx] = make_float4(lv[j].re.hi, lv[j].re.lo, lv[j].im.hi, lv[j].im.lo);
+                if (BWD)
+                    reinterpret_cast<float4 *>(hl)[idx] =
+                        make_float4(hv[j].re.hi, hv[j].re.lo, hv[j].im.hi, hv[j].im.lo);
+            } else {
+                lam[idx] = make_double2(df_join(lv[j].re.hi, lv[j].re.lo), df_join(lv[j].im.hi, lv[j].im.lo));
+                if (BWD)
+                    hl[idx] = make_double2(df_join(hv[j].re.hi, hv[j].re.lo), df_join(hv[j].im.hi, hv[j].im.lo));
+            }
+        }
+    }
+    if (BWD && w.ntrain > 0) {
+        __syncthreads();
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int t = warp; t < w.ntrain; t += kWinThreads / 32) {
+            EAcc<float> acc;
+#pragma unroll
+            for (int i = 0; i < kWinThreads / 32; i++) {
+                const float2 p = part[t * kWinThreads + i * 32 + lane];
+                df_add(p.x, p.y, acc.h, acc.l);
+            }
+            const double sum = acc.warp_sum();
+            if (lane == 0) {
+                const ETrain tr = train[w.tr0 + t];
+                bpart[(size_t)tr.slot * gridDim.x + blockIdx.x] = (double)tr.gscale * sum;
             }
         }
     }
@@ -144,16 +241,29 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
     PLK_TRY(device_ctx(lam->device, &d));
     cudaStream_t st = lam->stream;
     const uint64_t nu = lam->length >> kWinBits;
-    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)d->sm_count * 2,
+    const int per_sm = std::is_same<T, double>::value ? 1 : 2; // register budget of the df kernels
+    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)d->sm_count * per_sm,
                                                                     (nu + kWinThreads - 1) / kWinThreads));
-    std::vector<V> mats(P.mats.size() + P.gen.size());
-    for (size_t i = 0; i < P.mats.size(); i++) mats[i] = mk<V>((T)P.mats[i].x, (T)P.mats[i].y);
-    for (size_t i = 0; i < P.gen.size(); i++) mats[P.mats.size() + i] = mk<V>((T)P.gen[i].x, (T)P.gen[i].y);
+    // matrices: state precision for complex64, split double-floats for complex128
+    using M = typename std::conditional<std::is_same<T, double>::value, float4, V>::type;
+    std::vector<M> mats(P.mats.size() + P.gen.size());
+    auto conv = [](double2 z) {
+        if constexpr (std::is_same<T, double>::value) {
+            float4 f;
+            df_split_host(z.x, f.x, f.y);
+            df_split_host(z.y, f.z, f.w);
+            return f;
+        } else {
+            return mk<V>((T)z.x, (T)z.y);
+        }
+    };
+    for (size_t i = 0; i < P.mats.size(); i++) mats[i] = conv(P.mats[i]);
+    for (size_t i = 0; i < P.gen.size(); i++) mats[P.mats.size() + i] = conv(P.gen[i]);
     std::vector<EOp> ops = P.ops;
     for (auto &o : ops)
         if (o.gen >= 0) o.gen += (int32_t)P.mats.size();
     const size_t b_w = P.wins.size() * sizeof(EWin), b_o = ops.size() * sizeof(EOp);
-    const size_t b_t = std::max<size_t>(1, P.train.size()) * sizeof(ETrain), b_m = std::max<size_t>(1, mats.size()) * sizeof(V);
+    const size_t b_t = std::max<size_t>(1, P.train.size()) * sizeof(ETrain), b_m = std::max<size_t>(1, mats.size()) * sizeof(M);
     const size_t b_p = bwd ? (size_t)std::max(1, ntp) * grid * sizeof(double) : 0;
     const size_t b_j = bwd ? (size_t)std::max(1, ntp) * sizeof(double) : 0;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -167,7 +277,7 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
     p += al(b_o);
     ETrain *d_t = (ETrain *)p;
     p += al(b_t);
-    V *d_m = (V *)p;
+    M *d_m = (M *)p;
     p += al(b_m);
     double *d_p = (double *)p;
     p += al(b_p);
@@ -180,15 +290,41 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
     cp(d_w, P.wins.data(), b_w);
     cp(d_o, ops.data(), b_o);
     if (!P.train.empty()) cp(d_t, P.train.data(), P.train.size() * sizeof(ETrain));
-    if (!mats.empty()) cp(d_m, mats.data(), mats.size() * sizeof(V));
+    if (!mats.empty()) cp(d_m, mats.data(), mats.size() * sizeof(M));
     if (bwd && rc == PLK_OK && cudaMemsetAsync(d_p, 0, b_p, st) != cudaSuccess) rc = PLK_ERR_CUDA;
     V *lp = (V *)lam->data;
     V *hp = hl ? (V *)hl->data : nullptr;
     for (size_t wi = 0; wi < P.wins.size() && rc == PLK_OK; wi++) {
-        if (bwd)
-            k_state_window<T, true><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p);
-        else
-            k_state_window<T, false><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p);
+        // windows of one-wire ops and CNOTs only run the slim kernel
+        bool slim = true;
+        for (int k = 0; k < P.wins[wi].nops && slim; k++) {
+            const EOp &o = P.ops[P.wins[wi].op0 + k];
+            slim = (o.kind == EK_DENSE && o.K == 1) || o.kind == EK_CX || (o.kind == EK_DIAG && o.K == 1);
+        }
+        if constexpr (std::is_same<T, double>::value) {
+            const int in_df = wi > 0, out_df = wi + 1 < P.wins.size();
+#define PLK_WDF(B_, S_)                                                                                               \
+    k_state_window_df<B_, S_><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p, in_df,  \
+                                                           out_df)
+            if (bwd) {
+                if (slim) PLK_WDF(true, true);
+                else PLK_WDF(true, false);
+            } else {
+                if (slim) PLK_WDF(false, true);
+                else PLK_WDF(false, false);
+            }
+#undef PLK_WDF
+        } else {
+#define PLK_W(B_, S_) k_state_window<T, B_, S_><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p)
+            if (bwd) {
+                if (slim) PLK_W(true, true);
+                else PLK_W(true, false);
+            } else {
+                if (slim) PLK_W(false, true);
+                else PLK_W(false, false);
+            }
+#undef PLK_W
+        }
         if (cudaGetLastError() != cudaSuccess) rc = PLK_ERR_CUDA;
     }
     if (bwd && rc == PLK_OK && ntp > 0) {
@@ -209,7 +345,8 @@ bool window_path_enabled() { return g_window_path.load() != 0; }
 // Forward: the whole op list through windows (complex64).
 int window_apply_ops(plk_state s, const plk_op *ops, int nops, bool &handled) {
     handled = false;
-    if (!window_path_enabled() || s->dtype != PLK_C64 || nops < 4 || s->nq < 6 || s->nq > 32) return PLK_OK;
+    if (!window_path_enabled() || (s->dtype != PLK_C64 && !c128_use_df()) || nops < 4 || s->nq < 6 || s->nq > 32)
+        return PLK_OK;
     std::vector<XOp> xs;
     xs.reserve(nops * 3);
     for (int i = 0; i < nops; i++) {
@@ -230,7 +367,8 @@ int window_apply_ops(plk_state s, const plk_op *ops, int nops, bool &handled) {
     for (const auto &x : xs) PLK_TRY(wb.add(x));
     PLK_TRY(wb.close());
     handled = true;
-    return run_program<float>(s, nullptr, P, false, 0, nullptr);
+    return s->dtype == PLK_C64 ? run_program<float>(s, nullptr, P, false, 0, nullptr)
+                               : run_program<double>(s, nullptr, P, false, 0, nullptr);
 }
 
 // Backward sweep of the adjoint Jacobian with one observable (complex64);
@@ -238,7 +376,9 @@ int window_apply_ops(plk_state s, const plk_op *ops, int nops, bool &handled) {
 int window_adjoint(plk_state lam, plk_state hl, const plk_op *ops, int nops, const int64_t *tp, int ntp, double *jac,
                    bool &handled) {
     handled = false;
-    if (!window_path_enabled() || lam->dtype != PLK_C64 || lam->nq < 6 || lam->nq > 32 || ntp <= 0) return PLK_OK;
+    if (!window_path_enabled() || (lam->dtype != PLK_C64 && !c128_use_df()) || lam->nq < 6 || lam->nq > 32 ||
+        ntp <= 0)
+        return PLK_OK;
     int num_param_ops = 0;
     for (int i = 0; i < nops; i++)
         if (ops[i].num_params > 0) num_param_ops++;
@@ -275,7 +415,8 @@ int window_adjoint(plk_state lam, plk_state hl, const plk_op *ops, int nops, con
     PLK_TRY(wb.close());
     handled = true;
     std::vector<double> j(ntp, 0.0);
-    PLK_TRY(run_program<float>(lam, hl, P, true, ntp, j.data()));
+    if (lam->dtype == PLK_C64) PLK_TRY(run_program<float>(lam, hl, P, true, ntp, j.data()));
+    else PLK_TRY(run_program<double>(lam, hl, P, true, ntp, j.data()));
     for (int t = 0; t < ntp; t++) jac[t] = j[t];
     return PLK_OK;
 }

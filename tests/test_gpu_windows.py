@@ -1,9 +1,10 @@
 """GPU: register-window sweeps over one state (complex64 op lists and
 one-observable adjoint Jacobians) against the op-at-a-time path and the oracle.
 
-Tolerances: states within 5e-6 (complex64 rounding) of the op-at-a-time path
-and of the FP64 oracle; Jacobians within 1e-4 of the oracle and 2e-5 of the
-op-at-a-time complex64 path; window results are bitwise reproducible.
+Tolerances: complex64 states within 5e-6 of the op-at-a-time path and of the
+FP64 oracle, Jacobians within 1e-4 of the oracle and 2e-5 of the op-at-a-time
+path; complex128 (double-float windows) states within 1e-12 and Jacobians
+within 1e-10 of the oracle; window results are bitwise reproducible.
 """
 import ctypes as C
 
@@ -70,18 +71,22 @@ def oracle_forward(nq, ops):
     return psi
 
 
+STOL = {N.PLK_C64: 5e-6, N.PLK_C128: 1e-12}
+
+
+@pytest.mark.parametrize("dtype", [N.PLK_C64, N.PLK_C128])
 @pytest.mark.parametrize("nq", [6, 9, 12])
-def test_window_forward_matches_per_op_and_oracle(nq, window_switch):
+def test_window_forward_matches_per_op_and_oracle(nq, dtype, window_switch):
     rng = np.random.default_rng(100 + nq)
     ops = circuit_with_everything(nq, 120, rng)
     window_switch(True)
-    a = run_forward(nq, ops)
-    b = run_forward(nq, ops)
+    a = run_forward(nq, ops, dtype)
+    b = run_forward(nq, ops, dtype)
     window_switch(False)
-    c = run_forward(nq, ops)
+    c = run_forward(nq, ops, dtype)
     np.testing.assert_array_equal(a, b)
-    np.testing.assert_allclose(a, c, atol=5e-6, rtol=0)
-    np.testing.assert_allclose(a, oracle_forward(nq, ops), atol=5e-6, rtol=0)
+    np.testing.assert_allclose(a, c, atol=STOL[dtype], rtol=0)
+    np.testing.assert_allclose(a, oracle_forward(nq, ops), atol=STOL[dtype], rtol=0)
 
 
 def test_window_forward_layered_ansatz(window_switch):
@@ -92,6 +97,23 @@ def test_window_forward_layered_ansatz(window_switch):
     window_switch(True)
     a = run_forward(nq, ops)
     np.testing.assert_allclose(a, O.run_ops(O.zero_state(nq), ops), atol=5e-6, rtol=0)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_window_adjoint_c128_matches_oracle(seed, window_switch):
+    rng = np.random.default_rng(50 + seed)
+    nq = 7 + seed
+    ops = random_circuit(nq, 80, rng)
+    npar = sum(1 for o in ops if o[3])
+    trainable = sorted(int(x) for x in rng.choice(npar, max(1, npar * 2 // 3), replace=False))
+    obs = [("hamiltonian", [0.7, -0.4, 1.1],
+            [("named", "PauliZ", [1]), ("tensor", [("named", "PauliX", [0]), ("named", "PauliY", [3])]),
+             ("named", "PauliX", [nq - 1])])]
+    psi = O.run_ops(O.zero_state(nq), ops)
+    ref = O.adjoint_jacobian(psi, obs, ops, trainable)
+    window_switch(True)
+    jw = gpu_adjoint(psi, obs, ops, trainable, N.PLK_C128)
+    np.testing.assert_allclose(jw, ref, atol=1e-10, rtol=0)
 
 
 @pytest.mark.parametrize("seed", [0, 1, 2, 3])
