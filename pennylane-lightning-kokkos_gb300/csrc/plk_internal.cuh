@@ -61,8 +61,14 @@ struct DeviceCtx {
     int sm_count = 0;
     int max_threads_per_sm = 0;
     cudaStream_t stream = nullptr; // library stream of this device
+    cudaMemPool_t pool = nullptr;  // stream-ordered pool for state buffers (keeps freed blocks mapped)
 };
 int device_ctx(int device, DeviceCtx **out);
+
+// State buffers come from the device's pool: allocation on `stream`, ready
+// for any stream on return; release is stream ordered.
+int pool_alloc(int device, void **ptr, size_t bytes, cudaStream_t stream);
+void pool_free(void *ptr, cudaStream_t stream);
 
 constexpr int kThreads = 256;
 // Reductions use a fixed grid (a function of the device only) so that the

@@ -3,6 +3,7 @@
 // Replaces StateVectorKokkos's constructor / init / data movers
 // (simulator/StateVectorKokkos.hpp:140-574, 1596-1636) and the Kokkos
 // runtime configuration queries (util/GetConfigInfo.hpp).
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -42,10 +43,65 @@ int device_ctx(int device, DeviceCtx **out) {
         g_dev[device].sm_count = p.multiProcessorCount;
         g_dev[device].max_threads_per_sm = p.maxThreadsPerMultiProcessor;
         PLK_CUDA(cudaStreamCreateWithFlags(&g_dev[device].stream, cudaStreamNonBlocking));
+        // Freed state buffers stay mapped in the pool (up to the threshold),
+        // so creating a state of a size seen before costs no page mapping and
+        // destroying one no device-wide synchronisation.
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        PLK_CUDA(cudaMemPoolCreate(&g_dev[device].pool, &props));
+        uint64_t keep = std::min<uint64_t>(16ull << 30, p.totalGlobalMem / 8);
+        PLK_CUDA(cudaMemPoolSetAttribute(g_dev[device].pool, cudaMemPoolAttrReleaseThreshold, &keep));
         g_dev_init[device] = true;
     }
     *out = &g_dev[device];
     return PLK_OK;
+}
+
+int pool_alloc(int device, void **ptr, size_t bytes, cudaStream_t stream) {
+    DeviceCtx *d = nullptr;
+    PLK_TRY(device_ctx(device, &d));
+    *ptr = nullptr;
+    cudaError_t e = cudaMallocFromPoolAsync(ptr, bytes, d->pool, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        if (*ptr) cudaFreeAsync(*ptr, stream);
+        *ptr = nullptr;
+        PLK_FAIL(e == cudaErrorMemoryAllocation ? PLK_ERR_OUT_OF_MEMORY : PLK_ERR_CUDA,
+                 "allocation of " + std::to_string(bytes) + " bytes failed: " + cudaGetErrorString(e));
+    }
+    return PLK_OK;
+}
+
+void pool_free(void *ptr, cudaStream_t stream) {
+    if (ptr) cudaFreeAsync(ptr, stream);
+}
+
+// small pinned host buffers for reduction results, recycled across states
+namespace {
+std::mutex g_pinned_mutex;
+std::vector<double *> g_pinned_free;
+} // namespace
+
+static int pinned_get(double **out) {
+    {
+        std::lock_guard<std::mutex> lk(g_pinned_mutex);
+        if (!g_pinned_free.empty()) {
+            *out = g_pinned_free.back();
+            g_pinned_free.pop_back();
+            return PLK_OK;
+        }
+    }
+    PLK_CUDA(cudaMallocHost((void **)out, sizeof(double) * kMaxRedValues));
+    return PLK_OK;
+}
+
+static void pinned_put(double *p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(g_pinned_mutex);
+    g_pinned_free.push_back(p);
 }
 
 bool c128_use_df() {
@@ -206,11 +262,15 @@ PLK_API int plk_get_device_info(int device, plk_device_info *out) {
 }
 
 static int alloc_workspace(plk_state s) {
-    PLK_CUDA(cudaMalloc(&s->ws.d_partials, sizeof(double) * kMaxRedValues * kMaxRedBlocks));
-    PLK_CUDA(cudaMalloc(&s->ws.d_result, sizeof(double) * kMaxRedValues));
-    PLK_CUDA(cudaMalloc(&s->ws.d_counter, sizeof(unsigned int) * 4));
+    // partials, results and the ticket counter in one pool block
+    const size_t bp = sizeof(double) * kMaxRedValues * kMaxRedBlocks, br = sizeof(double) * kMaxRedValues;
+    void *blk = nullptr;
+    PLK_TRY(pool_alloc(s->device, &blk, bp + br + 256, s->stream));
+    s->ws.d_partials = (double *)blk;
+    s->ws.d_result = (double *)((char *)blk + bp);
+    s->ws.d_counter = (unsigned int *)((char *)blk + bp + br);
     PLK_CUDA(cudaMemsetAsync(s->ws.d_counter, 0, sizeof(unsigned int) * 4, s->stream));
-    PLK_CUDA(cudaMallocHost(&s->ws.h_result, sizeof(double) * kMaxRedValues));
+    PLK_TRY(pinned_get(&s->ws.h_result));
     return PLK_OK;
 }
 
@@ -218,11 +278,9 @@ static void free_state(plk_state s) {
     if (!s) return;
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
-    if (s->owned && s->data) cudaFree(s->data);
-    if (s->ws.d_partials) cudaFree(s->ws.d_partials);
-    if (s->ws.d_result) cudaFree(s->ws.d_result);
-    if (s->ws.d_counter) cudaFree(s->ws.d_counter);
-    if (s->ws.h_result) cudaFreeHost(s->ws.h_result);
+    if (s->owned && s->data) pool_free(s->data, s->stream);
+    if (s->ws.d_partials) pool_free(s->ws.d_partials, s->stream);
+    pinned_put(s->ws.h_result);
     s->data = nullptr;
     delete s;
 }
@@ -241,13 +299,11 @@ PLK_API int plk_state_create(int nq, int dtype, int device, plk_state *out) {
     s->dtype = dtype;
     s->length = 1ULL << nq;
     s->stream = d->stream;
-    cudaError_t e = cudaMalloc(&s->data, s->length * amp_bytes(dtype));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
+    if (pool_alloc(device, &s->data, s->length * amp_bytes(dtype), s->stream) != PLK_OK) {
+        const std::string err = last_error();
         s->data = nullptr;
         delete s;
-        PLK_FAIL(PLK_ERR_OUT_OF_MEMORY, "cudaMalloc of " + std::to_string(nq) + "-qubit state failed: " +
-                                            cudaGetErrorString(e));
+        PLK_FAIL(PLK_ERR_OUT_OF_MEMORY, "allocation of a " + std::to_string(nq) + "-qubit state failed: " + err);
     }
     int st = alloc_workspace(s);
     if (st == PLK_OK) st = fill_basis(s, 0);
