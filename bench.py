@@ -703,6 +703,18 @@ def run_precision(args, device, torch):
     return out
 
 
+# ------------------------------------------------------------- replicas --
+def aggregate_ranks(dist, torch, ms, nbytes, device="cpu"):
+    """Whole-job figures of independent replicas: the slowest rank's time and
+    the bytes of all ranks (value = all ranks' bytes / max time)."""
+    t = torch.tensor([ms, nbytes], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    sm = t.clone()
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(sm[1])
+
+
 # ------------------------------------------------------------------ main --
 def main(argv=None):
     args = parse_args(argv)
@@ -739,12 +751,7 @@ def main(argv=None):
     total_ms = sweep["total_ms"]
     total_bytes = sweep["total_bytes"]
     if dist is not None:
-        t = torch.tensor([total_ms, total_bytes], dtype=torch.float64, device=f"cuda:{device}")
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        sm = t.clone()
-        dist.all_reduce(sm, op=dist.ReduceOp.SUM)
-        total_ms, total_bytes = float(mx[0]), float(sm[1])
+        total_ms, total_bytes = aggregate_ranks(dist, torch, total_ms, total_bytes, f"cuda:{device}")
     value = total_bytes / (total_ms * 1e6)
 
     peak, peak_kind = peaks()
