@@ -663,13 +663,33 @@ __device__ __noinline__ void run_window(const EOp *__restrict__ ops, const c2_t<
             base = ((base ^ lo) << 1) | lo;
         }
         V lv[kWinAmps], hv[kWinAmps];
+        // complex64 in global memory with state bit 0 in the window: the
+        // pairs (j, j | 1) are adjacent, one 16-byte access each
+        const bool pairs = sizeof(T) == 4 && MODE == EM_GLOBAL && bb[0] == 1u;
+        if (pairs) {
 #pragma unroll
-        for (int j = 0; j < kWinAmps; j++) {
-            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
-                                 ((j & 8) ? bb[3] : 0);
-            lv[j] = act ? eld<T, MODE>(lam, idx) : mk<V>(0, 0);
-            if (BWD) hv[j] = act ? eld<T, MODE>(hl, idx) : mk<V>(0, 0);
-            else hv[j] = mk<V>(0, 0);
+            for (int j = 0; j < kWinAmps; j += 2) {
+                const uint32_t idx = base | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) | ((j & 8) ? bb[3] : 0);
+                const float4 a = act ? __ldcg(reinterpret_cast<const float4 *>(lam + idx)) : make_float4(0, 0, 0, 0);
+                lv[j] = mk<V>(a.x, a.y);
+                lv[j + 1] = mk<V>(a.z, a.w);
+                if (BWD) {
+                    const float4 b = act ? __ldcg(reinterpret_cast<const float4 *>(hl + idx)) : make_float4(0, 0, 0, 0);
+                    hv[j] = mk<V>(b.x, b.y);
+                    hv[j + 1] = mk<V>(b.z, b.w);
+                } else {
+                    hv[j] = hv[j + 1] = mk<V>(0, 0);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < kWinAmps; j++) {
+                const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
+                                     ((j & 8) ? bb[3] : 0);
+                lv[j] = act ? eld<T, MODE>(lam, idx) : mk<V>(0, 0);
+                if (BWD) hv[j] = act ? eld<T, MODE>(hl, idx) : mk<V>(0, 0);
+                else hv[j] = mk<V>(0, 0);
+            }
         }
         for (int k = 0; k < w.nops; k++) {
             const EOp op = ops[w.op0 + k];
@@ -681,7 +701,15 @@ __device__ __noinline__ void run_window(const EOp *__restrict__ ops, const c2_t<
                 part[op.red * NT + threadIdx.x] = acc.slot();
             }
         }
-        if (act) {
+        if (act && pairs) {
+#pragma unroll
+            for (int j = 0; j < kWinAmps; j += 2) {
+                const uint32_t idx = base | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) | ((j & 8) ? bb[3] : 0);
+                __stcg(reinterpret_cast<float4 *>(lam + idx), make_float4(lv[j].x, lv[j].y, lv[j + 1].x, lv[j + 1].y));
+                if (BWD)
+                    __stcg(reinterpret_cast<float4 *>(hl + idx), make_float4(hv[j].x, hv[j].y, hv[j + 1].x, hv[j + 1].y));
+            }
+        } else if (act) {
 #pragma unroll
             for (int j = 0; j < kWinAmps; j++) {
                 const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
