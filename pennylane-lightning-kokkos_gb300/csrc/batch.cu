@@ -167,8 +167,9 @@ static int compile_batch(plk_batch b) {
             WinBuilder wb{c.nq, bwd, b->h_win, b->h_ops, b->h_train, b->h_prep, b->h_gen, b->n_mats};
             const int w0 = (int)b->h_win.size();
             const int n = (int)c.ops.size();
+            std::vector<const XOp *> seq;
             if (!bwd) {
-                for (int k = 0; k < n; k++) PLK_TRY(wb.add(c.ops[k]));
+                for (int k = 0; k < n; k++) seq.push_back(&c.ops[k]);
             } else {
                 // ops before the first trainable op do not change the Jacobian
                 // (the reference loop ends there too, AdjointDiffKokkos.hpp:447)
@@ -178,8 +179,9 @@ static int compile_batch(plk_batch b) {
                         first = k;
                         break;
                     }
-                for (int k = n - 1; k >= first; k--) PLK_TRY(wb.add(c.ops[k]));
+                for (int k = n - 1; k >= first; k--) seq.push_back(&c.ops[k]);
             }
+            PLK_TRY(wb.add_scheduled(seq));
             PLK_TRY(wb.close());
             if (!bwd) {
                 e.fw0 = w0;

@@ -245,6 +245,64 @@ struct WinBuilder {
         return PLK_OK;
     }
 
+    bool fits(const XOp &o) const {
+        const bool tr = bwd && o.slot >= 0;
+        return popc(wbits | need(o)) <= kWinBits && (int)cur.size() < kMaxWinOps && !(tr && ntrain >= kMaxWinTrain);
+    }
+
+    // Packs `seq` (ops in application order) into windows, reordering ops
+    // that commute: an op may move ahead of earlier ops that share none of
+    // its wires (disjoint-wire ops commute, and so does the adjoint: a
+    // commuting U_m leaves <U_m H lambda | G U_m lambda> unchanged).  The
+    // schedule is a list schedule of the wire-dependency graph: the open
+    // window first takes ready ops that add no window bits, then the
+    // earliest ready op that still fits; when none fits it is closed.
+    int add_scheduled(const std::vector<const XOp *> &seq) {
+        const int n = (int)seq.size();
+        std::vector<std::vector<int>> succ(n);
+        std::vector<int> indeg(n, 0);
+        std::vector<int> last(32, -1);
+        for (int i = 0; i < n; i++) {
+            const XOp &o = *seq[i];
+            int ws[32];
+            int nw = 0;
+            if (o.kind == EK_PARITY)
+                for (int w : o.mrz_wires) ws[nw++] = w;
+            else
+                for (int j = 0; j < o.K; j++) ws[nw++] = o.wires[j];
+            for (int j = 0; j < nw; j++) {
+                const int p = last[ws[j]];
+                if (p >= 0 && (succ[p].empty() || succ[p].back() != i)) {
+                    succ[p].push_back(i);
+                    indeg[i]++;
+                }
+                last[ws[j]] = i;
+            }
+        }
+        std::vector<int> ready; // kept sorted by original index
+        for (int i = 0; i < n; i++)
+            if (indeg[i] == 0) ready.push_back(i);
+        int done = 0;
+        while (done < n) {
+            int pick = -1;
+            for (size_t r = 0; r < ready.size() && pick < 0; r++) // free ops first
+                if ((need(*seq[ready[r]]) & ~wbits) == 0 && fits(*seq[ready[r]])) pick = (int)r;
+            for (size_t r = 0; r < ready.size() && pick < 0; r++)
+                if (fits(*seq[ready[r]])) pick = (int)r;
+            if (pick < 0) {
+                PLK_TRY(close());
+                continue;
+            }
+            const int i = ready[pick];
+            ready.erase(ready.begin() + pick);
+            PLK_TRY(add(*seq[i]));
+            done++;
+            for (int s2 : succ[i])
+                if (--indeg[s2] == 0) ready.insert(std::lower_bound(ready.begin(), ready.end(), s2), s2);
+        }
+        return PLK_OK;
+    }
+
     int close() {
         if (cur.empty()) return PLK_OK;
         // pad with the highest unused state bits (low bits stay with the

@@ -364,7 +364,9 @@ int window_apply_ops(plk_state s, const plk_op *ops, int nops, bool &handled) {
     StateProgram P;
     WinBuilder wb{s->nq, false, P.wins, P.ops, P.train, P.prep, P.gen, P.n_mats};
     wb.hmats = &P.mats;
-    for (const auto &x : xs) PLK_TRY(wb.add(x));
+    std::vector<const XOp *> seq;
+    for (const auto &x : xs) seq.push_back(&x);
+    PLK_TRY(wb.add_scheduled(seq));
     PLK_TRY(wb.close());
     handled = true;
     return s->dtype == PLK_C64 ? run_program<float>(s, nullptr, P, false, 0, nullptr)
@@ -411,7 +413,9 @@ int window_adjoint(plk_state lam, plk_state hl, const plk_op *ops, int nops, con
     StateProgram P;
     WinBuilder wb{lam->nq, true, P.wins, P.ops, P.train, P.prep, P.gen, P.n_mats};
     wb.hmats = &P.mats;
-    for (const auto &x : xs) PLK_TRY(wb.add(x));
+    std::vector<const XOp *> seq;
+    for (const auto &x : xs) seq.push_back(&x);
+    PLK_TRY(wb.add_scheduled(seq));
     PLK_TRY(wb.close());
     handled = true;
     std::vector<double> j(ntp, 0.0);
