@@ -8,7 +8,7 @@
 // A layer of RY, RZ on every wire plus a CNOT ladder needs about 0.6 state
 // passes per wire instead of 3.
 //
-// Used (complex64; complex128 in double-float on the FP32 pipe, window_df.cuh,
+// Used (complex64; complex128 in double-float on the FP32 pipe, windows_df.cu,
 // unless PLK_C128_ARITH=fp64) by
 //   plk_apply_ops           (StateVectorKokkos::applyOperation over a tape,
 //                            StateVectorKokkos.hpp:585-676), and
@@ -28,7 +28,6 @@
 
 #include <type_traits>
 
-#include "window_df.cuh"
 #include "window_host.cuh"
 
 namespace plk {
@@ -70,98 +69,10 @@ __global__ void __launch_bounds__(kWinThreads, 2)
     }
 }
 
-// complex128 windows on the FP32 pipe (window_df.cuh).  Between windows of
-// one sweep the states stay in double-float form in their own buffers (a
-// {re.hi, re.lo, im.hi, im.lo} float4 has the size of a double2): the first
-// window splits the doubles (in_df = 0), the last joins them back
-// (out_df = 0), the ones between move raw pairs.
-template <bool BWD, bool SLIM>
-__global__ void __launch_bounds__(kWinThreads, 1)
-    k_state_window_df(double2 *lam, double2 *hl, int nq, const EWin *__restrict__ wins, int wi,
-                      const EOp *__restrict__ ops, const float4 *__restrict__ mats, const ETrain *__restrict__ train,
-                      double *__restrict__ bpart, int in_df, int out_df) {
-    __shared__ float2 part[kMaxWinTrain * kWinThreads];
-    const EWin w = wins[wi];
-    const int tid = threadIdx.x;
-    if (BWD)
-        for (int t = 0; t < w.ntrain; t++) part[t * kWinThreads + tid] = make_float2(0.0f, 0.0f);
-    const uint32_t nu = 1u << (nq - kWinBits);
-    const uint32_t bb[4] = {1u << w.rb[0], 1u << w.rb[1], 1u << w.rb[2], 1u << w.rb[3]};
-    const uint32_t tstep = gridDim.x * kWinThreads;
-    for (uint32_t u = blockIdx.x * kWinThreads + tid; u < nu; u += tstep) {
-        uint32_t base = u;
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const uint32_t lo = base & (bb[i] - 1);
-            base = ((base ^ lo) << 1) | lo;
-        }
-        CDF lv[kWinAmps], hv[kWinAmps];
-#pragma unroll
-        for (int j = 0; j < kWinAmps; j++) {
-            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
-                                 ((j & 8) ? bb[3] : 0);
-            if (in_df) {
-                const float4 a = reinterpret_cast<const float4 *>(lam)[idx];
-                lv[j] = {{a.x, a.y}, {a.z, a.w}};
-                if (BWD) {
-                    const float4 b = reinterpret_cast<const float4 *>(hl)[idx];
-                    hv[j] = {{b.x, b.y}, {b.z, b.w}};
-                } else {
-                    hv[j] = cdf_zero();
-                }
-            } else {
-                lv[j] = cdf_split(lam[idx]);
-                hv[j] = BWD ? cdf_split(hl[idx]) : cdf_zero();
-            }
-        }
-        for (int k = 0; k < w.nops; k++) {
-            const EOp op = ops[w.op0 + k];
-            DAcc acc, acc1;
-            if (BWD && op.red != 0xff) {
-                const float2 p = part[op.red * kWinThreads + tid];
-                acc.h = p.x;
-                acc.l = p.y;
-            }
-            window_op_df<BWD, SLIM>(op, lv, hv, base, bb, mats, acc, acc1);
-            if (BWD && op.red != 0xff) {
-                df_add(acc1.h, acc1.l, acc.h, acc.l);
-                part[op.red * kWinThreads + tid] = make_float2(acc.h, acc.l);
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < kWinAmps; j++) {
-            const uint32_t idx = base | ((j & 1) ? bb[0] : 0) | ((j & 2) ? bb[1] : 0) | ((j & 4) ? bb[2] : 0) |
-                                 ((j & 8) ? bb[3] : 0);
-            if (out_df) {
-                reinterpret_cast<float4 *>(lam)[idx] = make_float4(lv[j].re.hi, lv[j].re.lo, lv[j].im.hi, lv[j].im.lo);
-                if (BWD)
-                    reinterpret_cast<float4 *>(hl)[idx] =
-                        make_float4(hv[j].re.hi, hv[j].re.lo, hv[j].im.hi, hv[j].im.lo);
-            } else {
-                lam[idx] = make_double2(df_join(lv[j].re.hi, lv[j].re.lo), df_join(lv[j].im.hi, lv[j].im.lo));
-                if (BWD)
-                    hl[idx] = make_double2(df_join(hv[j].re.hi, hv[j].re.lo), df_join(hv[j].im.hi, hv[j].im.lo));
-            }
-        }
-    }
-    if (BWD && w.ntrain > 0) {
-        __syncthreads();
-        const int lane = tid & 31, warp = tid >> 5;
-        for (int t = warp; t < w.ntrain; t += kWinThreads / 32) {
-            EAcc<float> acc;
-#pragma unroll
-            for (int i = 0; i < kWinThreads / 32; i++) {
-                const float2 p = part[t * kWinThreads + i * 32 + lane];
-                df_add(p.x, p.y, acc.h, acc.l);
-            }
-            const double sum = acc.warp_sum();
-            if (lane == 0) {
-                const ETrain tr = train[w.tr0 + t];
-                bpart[(size_t)tr.slot * gridDim.x + blockIdx.x] = (double)tr.gscale * sum;
-            }
-        }
-    }
-}
+// complex128 windows (windows_df.cu)
+void launch_window_df(bool bwd, bool slim, int grid, cudaStream_t st, double2 *lam, double2 *hl, int nq,
+                      const EWin *wins, int wi, const EOp *ops, const float4 *mats, const ETrain *train,
+                      double *bpart, int in_df, int out_df);
 
 // jac[s] = sum over blocks, in block order
 __global__ void k_window_jac(const double *__restrict__ bpart, int nblocks, int ntp, double *__restrict__ jac) {
@@ -282,6 +193,7 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
     double *d_p = (double *)p;
     p += al(b_p);
     double *d_j = (double *)p;
+
     int rc = PLK_OK;
     auto cp = [&](void *dst, const void *src, size_t n) {
         if (rc == PLK_OK && n && cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, st) != cudaSuccess)
@@ -292,28 +204,23 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
     if (!P.train.empty()) cp(d_t, P.train.data(), P.train.size() * sizeof(ETrain));
     if (!mats.empty()) cp(d_m, mats.data(), mats.size() * sizeof(M));
     if (bwd && rc == PLK_OK && cudaMemsetAsync(d_p, 0, b_p, st) != cudaSuccess) rc = PLK_ERR_CUDA;
+
     V *lp = (V *)lam->data;
     V *hp = hl ? (V *)hl->data : nullptr;
+    auto window_is_slim = [&](size_t wi) {
+        for (int k = 0; k < P.wins[wi].nops; k++) {
+            const EOp &o = P.ops[P.wins[wi].op0 + k];
+            if (!((o.kind == EK_DENSE && o.K == 1) || o.kind == EK_CX || (o.kind == EK_DIAG && o.K == 1)))
+                return false;
+        }
+        return true;
+    };
     for (size_t wi = 0; wi < P.wins.size() && rc == PLK_OK; wi++) {
         // windows of one-wire ops and CNOTs only run the slim kernel
-        bool slim = true;
-        for (int k = 0; k < P.wins[wi].nops && slim; k++) {
-            const EOp &o = P.ops[P.wins[wi].op0 + k];
-            slim = (o.kind == EK_DENSE && o.K == 1) || o.kind == EK_CX || (o.kind == EK_DIAG && o.K == 1);
-        }
+        const bool slim = window_is_slim(wi);
         if constexpr (std::is_same<T, double>::value) {
             const int in_df = wi > 0, out_df = wi + 1 < P.wins.size();
-#define PLK_WDF(B_, S_)                                                                                               \
-    k_state_window_df<B_, S_><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p, in_df,  \
-                                                           out_df)
-            if (bwd) {
-                if (slim) PLK_WDF(true, true);
-                else PLK_WDF(true, false);
-            } else {
-                if (slim) PLK_WDF(false, true);
-                else PLK_WDF(false, false);
-            }
-#undef PLK_WDF
+launch_window_df(bwd, slim, grid, st, lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p, in_df, out_df);
         } else {
 #define PLK_W(B_, S_) k_state_window<T, B_, S_><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p)
             if (bwd) {

@@ -174,3 +174,4 @@ def test_window_switch_roundtrip(window_switch):
     window_switch(True)
     N.check(N.lib.plk_get_window_path(C.byref(v)))
     assert v.value == 1
+
