@@ -383,7 +383,8 @@ __device__ void run_circuit(const EngArgs<T> &a, int cid, int rank, int C, c2_t<
     esync(C);
     for (int k = 0; k < ci.nfw; k++) {
         const EWin w = a.win[ci.fw0 + k];
-        run_window<T, NT, MODE, false>(a.ops, a.mats, w, ci.nq, lam, hl, t0, tstep, part);
+        if (w.flags & 1) run_window<T, NT, MODE, false, true>(a.ops, a.mats, w, ci.nq, lam, hl, t0, tstep, part);
+        else run_window<T, NT, MODE, false, false>(a.ops, a.mats, w, ci.nq, lam, hl, t0, tstep, part);
         esync(C);
     }
     h_pass<T, NT, MODE>(a, ci, lam, hl, t0, tstep, misc, rank, C);
@@ -398,7 +399,8 @@ __device__ void run_circuit(const EngArgs<T> &a, int cid, int rank, int C, c2_t<
         // two partial buffers: finalizing window k overlaps window k + 1;
         // one buffer: a barrier after finalizing
         typename EAcc<T>::Slot *rb = part + (NBUF == 2 ? (k & 1) : 0) * kMaxWinTrain * NT;
-        run_window<T, NT, MODE, true>(a.ops, a.mats, w, ci.nq, lam, hl, t0, tstep, rb);
+        if (w.flags & 1) run_window<T, NT, MODE, true, true>(a.ops, a.mats, w, ci.nq, lam, hl, t0, tstep, rb);
+        else run_window<T, NT, MODE, true, false>(a.ops, a.mats, w, ci.nq, lam, hl, t0, tstep, rb);
         esync(C);
         finalize_window<T, NT>(a, ci, w, rb, rank, C);
         if (NBUF == 1) esync(C);

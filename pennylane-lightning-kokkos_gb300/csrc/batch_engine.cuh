@@ -66,6 +66,7 @@ struct EOp {
 
 struct EWin {
     uint8_t rb[4];   // state bits of register bits 0..3 (ascending)
+    int32_t flags;   // bit 0: only one-wire dense ops, one-wire diagonals and CNOTs (slim)
     int32_t op0;     // ops [op0, op0 + nops)
     int32_t nops;
     int32_t tr0;     // trainable table [tr0, tr0 + ntrain)

@@ -317,6 +317,10 @@ struct WinBuilder {
                 win.rb[r] = (uint8_t)bit;
                 pos[bit] = r++;
             }
+        win.flags = 1;
+        for (const XOp *op : cur)
+            if (!((op->kind == EK_DENSE && op->K == 1) || op->kind == EK_CX || (op->kind == EK_DIAG && op->K == 1)))
+                win.flags = 0;
         win.op0 = (int)ops.size();
         win.nops = (int)cur.size();
         win.tr0 = (int)train.size();

@@ -69,10 +69,14 @@ __global__ void __launch_bounds__(kWinThreads, 2)
     }
 }
 
-// complex128 windows (windows_df.cu)
-void launch_window_df(bool bwd, bool slim, int grid, cudaStream_t st, double2 *lam, double2 *hl, int nq,
-                      const EWin *wins, int wi, const EOp *ops, const float4 *mats, const ETrain *train,
-                      double *bpart, int in_df, int out_df);
+// complex128 windows (windows_df.cu, windows_df_fwd.cu; the slim variant of
+// the complex64 kernels measured no faster there, double-float work dominates)
+void launch_window_df_bwd(int grid, cudaStream_t st, double2 *lam, double2 *hl, int nq, const EWin *wins, int wi,
+                          const EOp *ops, const float4 *mats, const ETrain *train, double *bpart, int in_df,
+                          int out_df);
+void launch_window_df_fwd(int grid, cudaStream_t st, double2 *lam, double2 *hl, int nq, const EWin *wins, int wi,
+                          const EOp *ops, const float4 *mats, const ETrain *train, double *bpart, int in_df,
+                          int out_df);
 
 // jac[s] = sum over blocks, in block order
 __global__ void k_window_jac(const double *__restrict__ bpart, int nblocks, int ntp, double *__restrict__ jac) {
@@ -207,20 +211,13 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
 
     V *lp = (V *)lam->data;
     V *hp = hl ? (V *)hl->data : nullptr;
-    auto window_is_slim = [&](size_t wi) {
-        for (int k = 0; k < P.wins[wi].nops; k++) {
-            const EOp &o = P.ops[P.wins[wi].op0 + k];
-            if (!((o.kind == EK_DENSE && o.K == 1) || o.kind == EK_CX || (o.kind == EK_DIAG && o.K == 1)))
-                return false;
-        }
-        return true;
-    };
     for (size_t wi = 0; wi < P.wins.size() && rc == PLK_OK; wi++) {
         // windows of one-wire ops and CNOTs only run the slim kernel
-        const bool slim = window_is_slim(wi);
+        const bool slim = P.wins[wi].flags & 1;
         if constexpr (std::is_same<T, double>::value) {
             const int in_df = wi > 0, out_df = wi + 1 < P.wins.size();
-launch_window_df(bwd, slim, grid, st, lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p, in_df, out_df);
+if (bwd) launch_window_df_bwd(grid, st, lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p, in_df, out_df);
+            else launch_window_df_fwd(grid, st, lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p, in_df, out_df);
         } else {
 #define PLK_W(B_, S_) k_state_window<T, B_, S_><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p)
             if (bwd) {
