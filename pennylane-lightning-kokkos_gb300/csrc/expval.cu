@@ -91,14 +91,32 @@ __global__ void __launch_bounds__(kThreads)
             const uint64_t k = k0 + u * step;
             v[u] = k < n ? sv[k] : mk<c2_t<T>>(0, 0);
         }
+        if constexpr (sizeof(T) == 4) {
+            // complex64: the U amplitudes' signed |a|^2 summed in FP32, the
+            // partial added in double-float (error of a partial ~2^-22 of
+            // its size, below the state's own rounding)
+            float t[NV];
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            const uint64_t k = k0 + u * step;
-            const DF p = df_norm2(to_cdf(v[u]));
+            for (int w = 0; w < NV; w++) t[w] = 0.0f;
 #pragma unroll
-            for (int w = 0; w < NV; w++) {
-                if (__popcll(k & zm[w]) & 1) dacc[w].sub(p);
-                else dacc[w].add(p);
+            for (int u = 0; u < U; u++) {
+                const uint64_t k = k0 + u * step;
+                const float p = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
+#pragma unroll
+                for (int w = 0; w < NV; w++) t[w] += (__popcll(k & zm[w]) & 1) ? -p : p;
+            }
+#pragma unroll
+            for (int w = 0; w < NV; w++) dacc[w].add(DF{t[w], 0.0f});
+        } else {
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const uint64_t k = k0 + u * step;
+                const DF p = df_norm2(to_cdf(v[u]));
+#pragma unroll
+                for (int w = 0; w < NV; w++) {
+                    if (__popcll(k & zm[w]) & 1) dacc[w].sub(p);
+                    else dacc[w].add(p);
+                }
             }
         }
     }
@@ -287,7 +305,34 @@ __global__ void __launch_bounds__(kThreads)
     // coefficients of the group as double-floats (split once per thread)
     DAcc total;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    if (x == 0) {
+    if constexpr (sizeof(T) == 4) {
+        // complex64: each amplitude (pair)'s contribution formed in FP32,
+        // accumulated in double-float
+        if (x == 0) {
+            for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
+                const float2 a = sv[k];
+                float f = 0.0f;
+                for (int t = 0; t < nt; t++) f += (__popcll(k & sterm[t].z) & 1) ? -sterm[t].crh : sterm[t].crh;
+                total.add(DF{fmaf(a.x, a.x, a.y * a.y) * f, 0.0f});
+            }
+        } else {
+            const uint64_t half = n >> 1;
+            for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < half; g += step) {
+                const uint64_t m = ((g & ~pmask_lo) << 1) | (g & pmask_lo);
+                const uint64_t mp = m ^ x;
+                const float2 a = sv[m], b = sv[mp];
+                float f1 = 0.0f, f2 = 0.0f;
+                for (int t = 0; t < nt; t++) {
+                    const PauliTerm tt = sterm[t];
+                    const bool s1 = __popcll(mp & tt.z) & 1, s0 = __popcll(m & tt.z) & 1;
+                    if (s1 == s0) f1 += s0 ? -2.0f * tt.crh : 2.0f * tt.crh;
+                    else f2 += s0 ? -2.0f * tt.cih : 2.0f * tt.cih;
+                }
+                const float re = fmaf(a.x, b.x, a.y * b.y), im = fmaf(a.x, b.y, -a.y * b.x);
+                total.add(DF{fmaf(re, f1, im * f2), 0.0f});
+            }
+        }
+    } else if (x == 0) {
         for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
             const DF p = df_norm2(to_cdf(sv[k]));
             DAcc f;
