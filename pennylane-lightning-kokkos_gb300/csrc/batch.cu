@@ -296,11 +296,14 @@ __global__ void k_batch_prepare(const EPrep *__restrict__ prep, int nprep, const
     }
 }
 
-// C > 1 only for global states shared by a cluster
+// C > 1 only for global states shared by a cluster.  The cluster barrier
+// arrives with release and waits with acquire semantics at cluster scope, so
+// the window's global writes of every CTA are visible to the whole cluster
+// after it (the accesses themselves bypass L1).
 __device__ __forceinline__ void esync(int C) {
     if (C > 1) {
-        __threadfence();
-        cg::this_cluster().sync();
+        asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+        asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
     } else {
         __syncthreads();
     }
