@@ -77,11 +77,13 @@ def parse_args(argv=None):
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--no-plain20", action="store_true")
-    ap.add_argument("--only", choices=["adjoint", "batch", "plain20", "precision"], default=None,
+    ap.add_argument("--only", choices=["adjoint", "batch", "plain20", "precision", "kernels"], default=None,
                     help="run one secondary config alone and print its JSON (profiling and spot checks)")
     ap.add_argument("--no-tune", action="store_true", help="batch: fixed launch configuration instead of autotuning")
     ap.add_argument("--precision", action="store_true",
                     help="also run the equal-bytes precision config (32-qubit complex64 vs 31-qubit complex128)")
+    ap.add_argument("--census-nq", type=int, default=26, help="--only kernels: state size in qubits")
+    ap.add_argument("--census-reps", type=int, default=3, help="--only kernels: timed calls per entry point")
     return ap.parse_args(argv)
 
 
@@ -703,6 +705,143 @@ def run_precision(args, device, torch):
     return out
 
 
+# ---------------------------------------------------------- kernel census --
+def run_kernels(args, device, torch):
+    """One call of every C-ABI entry point family on a state larger than L2
+    (default 26 qubits: 1 GiB complex128, 512 MiB complex64), timed with CUDA
+    events on the state's stream (median of ``--census-reps``).  Each line
+    gives the algorithmic bytes of the call (the state passes the operation
+    needs at minimum) and the achieved GB/s; calls that return host arrays
+    (probs, CDF, samples) include their device-to-host copy in the time."""
+    from pennylane_lightning_kokkos import _native as N
+    from pennylane_lightning_kokkos.circuits import random_pauli_words
+
+    nq, reps = args.census_nq, max(1, args.census_reps)
+    n = 1 << nq
+    rng = np.random.default_rng(7)
+    stream = torch.cuda.Stream(device=device)
+    i64 = lambda a: np.ascontiguousarray(a, dtype=np.int64)
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    P64 = lambda a: a.ctypes.data_as(C.POINTER(C.c_int64))
+    PD = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+
+    def haar(k):
+        z = rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))
+        q, r = np.linalg.qr(z)
+        return np.ascontiguousarray(q * (np.diag(r) / np.abs(np.diag(r))), dtype=np.complex128)
+
+    words = random_pauli_words(nq, 20, seed=7)
+    co = f64([c for c, _, _ in words])
+    of = i64(np.cumsum([0] + [len(w) for _, w, _ in words]))
+    wi = i64([x for _, w, _ in words for x in w])
+    le = "".join(l for _, _, l in words).encode()
+
+    def xmask(w, l):
+        return sum(1 << (nq - 1 - x) for x, c in zip(w, l) if c in "XY")
+
+    npass_words = len({xmask(w, l) for _, w, l in words})
+    m3, m2 = haar(3), haar(2)
+    u = f64(rng.random(1 << 20))
+    shots_out = np.empty((1 << 20) * nq, dtype=np.int64)
+    probs_full = np.empty(n, dtype=np.float64)
+    probs_m = np.empty(1 << 14, dtype=np.float64)
+    wm = i64(rng.permutation(nq)[:14])
+
+    out = {"qubits": nq, "reps": reps, "timing": "CUDA events on the state's stream, median of reps",
+           "calls": {}}
+    for dtype, dname, sz in ((N.PLK_C128, "c128", 16), (N.PLK_C64, "c64", 8)):
+        S = n * sz
+        hs = []
+        for _ in range(2):
+            h = C.c_void_p()
+            N.check(N.lib.plk_state_create(nq, dtype, device, C.byref(h)))
+            N.check(N.lib.plk_state_set_stream(h, C.c_void_p(stream.cuda_stream)))
+            hs.append(h)
+        a, b = hs
+        hw = i64([0])
+        for w in range(nq):
+            hw[0] = w
+            N.check(N.lib.plk_apply_gate(a, N.GATE_ID["Hadamard"], P64(hw), 1, 0, None, 0))
+        N.check(N.lib.plk_state_copy(b, a))
+        keep = []
+
+        def gate(name, wires, params=()):
+            w, p = i64(wires), f64(list(params) or [0.0])
+            keep.extend([w, p])
+            g = N.GATE_ID[name]
+            return lambda: N.check(N.lib.plk_apply_gate(a, g, P64(w), len(w), 0, PD(p), len(params)))
+
+        def matrix(m, wires):
+            w = i64(wires)
+            keep.extend([w, m])
+            return lambda: N.check(N.lib.plk_apply_matrix(a, m.ctypes.data_as(C.POINTER(C.c_double)), P64(w),
+                                                          len(w), 0))
+
+        sc, v, vr, vi = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        zb = np.array([N.GATE_ID["PauliZ"]] * 20, dtype=np.int32)
+        zw = i64(range(20))
+        lo, mid, hi = nq - 3, nq // 2, 1  # wire -> rev bit: 2, ~n/2, n-2
+        calls = [
+            ("reset (|0>)", lambda: N.check(N.lib.plk_state_reset(a)), S),
+            ("PauliX low wire", gate("PauliX", [lo]), 2 * S),
+            ("PauliX high wire", gate("PauliX", [hi]), 2 * S),
+            ("Hadamard", gate("Hadamard", [mid]), 2 * S),
+            ("RX", gate("RX", [mid], [0.3]), 2 * S),
+            ("CNOT", gate("CNOT", [hi, lo]), S),
+            ("CRY", gate("CRY", [lo, mid], [0.4]), S),
+            ("IsingXX", gate("IsingXX", [mid, hi], [0.5]), 2 * S),
+            ("SingleExcitation", gate("SingleExcitation", [lo, hi], [0.6]), S),
+            ("DoubleExcitation", gate("DoubleExcitation", [0, 5, 9, lo], [0.7]), S // 4),
+            ("Toffoli", gate("Toffoli", [hi, mid, lo]), S // 2),
+            ("CSWAP", gate("CSWAP", [hi, mid, lo]), S // 2),
+            ("MultiRZ (5 wires)", gate("MultiRZ", [0, 3, mid, lo, nq - 1], [0.8]), 2 * S),
+            ("Haar 2-qubit matrix", matrix(m2, [mid, lo]), 2 * S),
+            ("Haar 3-qubit matrix", matrix(m3, [hi, mid, lo]), 2 * S),
+            ("generator IsingXX", lambda: N.check(N.lib.plk_apply_generator(a, N.GATE_ID["IsingXX"], P64(zw), 2, 0,
+                                                                            C.byref(sc))), 2 * S),
+            ("expval PauliZ", lambda: N.check(N.lib.plk_expval_named(a, N.GATE_ID["PauliZ"], P64(zw), 1,
+                                                                     C.byref(v))), S),
+            ("expval PauliX", lambda: N.check(N.lib.plk_expval_named(a, N.GATE_ID["PauliX"], P64(zw), 1,
+                                                                     C.byref(v))), S),
+            ("expval 20 x PauliZ (one pass)", lambda: N.check(N.lib.plk_expval_named_batch(
+                a, 20, zb.ctypes.data_as(C.POINTER(C.c_int32)), P64(zw), PD(probs_m))), S),
+            ("expval 2-qubit matrix", lambda: N.check(N.lib.plk_expval_matrix(
+                a, m2.ctypes.data_as(C.POINTER(C.c_double)), P64(i64([mid, lo])), 2, C.byref(v))), S),
+            ("expval 3-qubit matrix", lambda: N.check(N.lib.plk_expval_matrix(
+                a, m3.ctypes.data_as(C.POINTER(C.c_double)), P64(i64([hi, mid, lo])), 3, C.byref(v))), S),
+            (f"expval 20 Pauli words ({npass_words} passes)", lambda: N.check(N.lib.plk_expval_pauli_sum(
+                a, len(co), PD(co), P64(of), P64(wi), le, C.byref(v))), npass_words * S),
+            ("apply 20 Pauli words (H|psi>)", lambda: N.check(N.lib.plk_apply_pauli_sum(
+                b, a, len(co), PD(co), P64(of), P64(wi), le)), 2 * S),
+            ("inner product", lambda: N.check(N.lib.plk_inner_product(a, b, C.byref(vr), C.byref(vi))), 2 * S),
+            ("axpy", lambda: N.check(N.lib.plk_state_axpy(b, 0.5, 0.25, a)), 3 * S),
+            ("copy", lambda: N.check(N.lib.plk_state_copy(b, a)), 2 * S),
+            ("probs() to host", lambda: N.check(N.lib.plk_probs(a, None, 0, PD(probs_full))), S + n * 8),
+            ("probs(14 wires) to host", lambda: N.check(N.lib.plk_probs(a, P64(wm), 14, PD(probs_m))), S),
+            ("CDF to host", lambda: N.check(N.lib.plk_cdf(a, PD(probs_full))), 2 * S + n * 8),
+            ("sample 2^20 shots from uniforms", lambda: N.check(N.lib.plk_sample_from_uniforms(
+                a, PD(u), len(u), P64(shots_out))), 2 * S),
+        ]
+        res = {}
+        for name, fn, nbytes in calls:
+            fn()  # warm-up
+            ts = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize(device)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize(device)
+                ts.append(e0.elapsed_time(e1))
+            ms = statistics.median(ts)
+            res[name] = {"ms": ms, "algorithmic_bytes": nbytes, "GBps": nbytes / (ms * 1e6)}
+        for h in hs:
+            N.lib.plk_state_destroy(h)
+        out["calls"][dname] = res
+    return out
+
+
 # ------------------------------------------------------------- replicas --
 def aggregate_ranks(dist, torch, ms, nbytes, device="cpu"):
     """Whole-job figures of independent replicas: the slowest rank's time and
@@ -734,7 +873,8 @@ def main(argv=None):
     torch.cuda.set_device(device)
     if args.only:
         if rank == 0:
-            fn = {"adjoint": run_adjoint, "batch": run_batch, "plain20": run_plain20, "precision": run_precision}
+            fn = {"adjoint": run_adjoint, "batch": run_batch, "plain20": run_plain20, "precision": run_precision,
+                  "kernels": run_kernels}
             print(json.dumps({args.only: fn[args.only](args, device, torch)}), flush=True)
         return 0
     dist = None

@@ -74,50 +74,117 @@ __global__ void __launch_bounds__(kThreads)
 
 // Diagonal observables in one pass: value v = sum_k |psi_k|^2 * sign_v(k) with
 // sign_v(k) = (-1)^popcount(k & zmask_v) (Identity: zmask 0; PauliZ: one bit).
+// A thread takes "quads" of amplitudes base + 32 j (j = 0..3, base with bits
+// 5 and 6 clear), so each load instruction of a warp reads 32 consecutive
+// amplitudes.  The four weights of a quad are combined once into the Walsh
+// sums W[s] = sum_j (-1)^popcount(j & s) p_j; an observable then needs the
+// parity of base & zmask and W[(zmask >> 5) & 3]: one add per observable per
+// four amplitudes.  Loads of the next quads are issued before the current
+// ones are evaluated.
+template <class T> struct Quad {
+    c2_t<T> v[4];
+};
+
+template <class T>
+__device__ __forceinline__ void diag_load_quad(const c2_t<T> *__restrict__ sv, uint64_t n, uint64_t q, Quad<T> &d,
+                                               uint64_t &base) {
+    base = ((q >> 5) << 7) | (q & 31);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const uint64_t k = base + 32 * j;
+        d.v[j] = k < n ? sv[k] : mk<c2_t<T>>(0, 0);
+    }
+}
+
+// up to 16 Z masks, passed by value (no allocation or copy per call)
+struct DiagMasks {
+    uint64_t z[16];
+};
+
 template <class T, int NV>
 __global__ void __launch_bounds__(kThreads)
-    k_expval_diag(const c2_t<T> *__restrict__ sv, uint64_t n, const uint64_t *__restrict__ zmask, int nv,
-                  double *partials, double *result, unsigned *counter) {
+    k_expval_diag(const c2_t<T> *__restrict__ sv, uint64_t n, const DiagMasks zmask, int nv, double *partials,
+                  double *result, unsigned *counter) {
+    constexpr int U = sizeof(T) == 8 ? 1 : 2; // quads per batch
     __shared__ uint64_t zm[NV];
-    for (int v = threadIdx.x; v < NV; v += blockDim.x) zm[v] = v < nv ? zmask[v] : 0;
+    __shared__ int zs[NV];
+    for (int v = threadIdx.x; v < NV; v += blockDim.x) {
+        const uint64_t z = v < nv ? zmask.z[v] : 0;
+        zm[v] = z & ~(3ULL << 5);
+        zs[v] = (int)((z >> 5) & 3);
+    }
     __syncthreads();
     DAcc dacc[NV];
-    constexpr int U = 4; // amplitudes in flight per thread
+    const uint64_t nquads = ((n + 127) >> 7) << 5;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t k0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += step * U) {
-        c2_t<T> v[U];
+    Quad<T> cur[U];
+    uint64_t cb[U];
+    uint64_t q0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
 #pragma unroll
-        for (int u = 0; u < U; u++) {
-            const uint64_t k = k0 + u * step;
-            v[u] = k < n ? sv[k] : mk<c2_t<T>>(0, 0);
-        }
+    for (int u = 0; u < U; u++) diag_load_quad(sv, q0 + u * step < nquads ? n : 0, q0 + u * step, cur[u], cb[u]);
+    for (; q0 < nquads; q0 += step * U) {
+        Quad<T> nxt[U];
+        uint64_t nb[U];
+        const uint64_t q1 = q0 + step * U;
+#pragma unroll
+        for (int u = 0; u < U; u++) diag_load_quad(sv, q1 + u * step < nquads ? n : 0, q1 + u * step, nxt[u], nb[u]);
         if constexpr (sizeof(T) == 4) {
-            // complex64: the U amplitudes' signed |a|^2 summed in FP32, the
-            // partial added in double-float (error of a partial ~2^-22 of
-            // its size, below the state's own rounding)
+            // complex64: Walsh sums and signed partials in FP32, one
+            // double-float add per observable per batch
             float t[NV];
 #pragma unroll
             for (int w = 0; w < NV; w++) t[w] = 0.0f;
 #pragma unroll
             for (int u = 0; u < U; u++) {
-                const uint64_t k = k0 + u * step;
-                const float p = fmaf(v[u].x, v[u].x, v[u].y * v[u].y);
+                float p[4];
 #pragma unroll
-                for (int w = 0; w < NV; w++) t[w] += (__popcll(k & zm[w]) & 1) ? -p : p;
+                for (int j = 0; j < 4; j++) p[j] = fmaf(cur[u].v[j].x, cur[u].v[j].x, cur[u].v[j].y * cur[u].v[j].y);
+                const float a = p[0] + p[1], b = p[0] - p[1], c = p[2] + p[3], d = p[2] - p[3];
+                const float W0 = a + c, W1 = b + d, W2 = a - c, W3 = b - d;
+#pragma unroll
+                for (int w = 0; w < NV; w++) {
+                    const int sel = zs[w];
+                    const float val = sel == 0 ? W0 : (sel == 1 ? W1 : (sel == 2 ? W2 : W3));
+                    t[w] += (__popcll(cb[u] & zm[w]) & 1) ? -val : val;
+                }
             }
 #pragma unroll
             for (int w = 0; w < NV; w++) dacc[w].add(DF{t[w], 0.0f});
         } else {
 #pragma unroll
             for (int u = 0; u < U; u++) {
-                const uint64_t k = k0 + u * step;
-                const DF p = df_norm2(to_cdf(v[u]));
+                DF p[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) p[j] = df_norm2(to_cdf(cur[u].v[j]));
+                // Walsh sums in double-float
+                float ah = p[0].hi, al = p[0].lo, bh = p[0].hi, bl = p[0].lo;
+                df_add(p[1].hi, p[1].lo, ah, al);
+                df_add(-p[1].hi, -p[1].lo, bh, bl);
+                float ch = p[2].hi, cl = p[2].lo, dh = p[2].hi, dl = p[2].lo;
+                df_add(p[3].hi, p[3].lo, ch, cl);
+                df_add(-p[3].hi, -p[3].lo, dh, dl);
+                float w0h = ah, w0l = al, w2h = ah, w2l = al, w1h = bh, w1l = bl, w3h = bh, w3l = bl;
+                df_add(ch, cl, w0h, w0l);
+                df_add(-ch, -cl, w2h, w2l);
+                df_add(dh, dl, w1h, w1l);
+                df_add(-dh, -dl, w3h, w3l);
 #pragma unroll
                 for (int w = 0; w < NV; w++) {
-                    if (__popcll(k & zm[w]) & 1) dacc[w].sub(p);
-                    else dacc[w].add(p);
+                    const int sel = zs[w];
+                    float vh = sel == 0 ? w0h : (sel == 1 ? w1h : (sel == 2 ? w2h : w3h));
+                    float vl = sel == 0 ? w0l : (sel == 1 ? w1l : (sel == 2 ? w2l : w3l));
+                    if (__popcll(cb[u] & zm[w]) & 1) {
+                        vh = -vh;
+                        vl = -vl;
+                    }
+                    dacc[w].add(DF{vh, vl});
                 }
             }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            cur[u] = nxt[u];
+            cb[u] = nb[u];
         }
     }
     double acc[NV];
@@ -126,41 +193,87 @@ __global__ void __launch_bounds__(kThreads)
     block_reduce_finish<NV>(acc, partials, result, counter, 1.0, nv);
 }
 
-// <psi| M |psi> for a 1- or 2-wire matrix (ExpValFunctors.hpp:155-250).
+// Re<psi| M |psi> for a matrix on K = 1, 2 or 3 wires (ExpValFunctors.hpp:155-250;
+// MeasuresKokkos.hpp:318-346 for K >= 3).  Re<v|M|v> = <v|H|v> with the
+// Hermitian part H = (M + M^dag)/2, so each group of 2^K amplitudes adds
+//   sum_r H_rr |v_r|^2 + sum_{r<c} (a_rc Re(conj(v_r) v_c) + b_rc Im(conj(v_r) v_c))
+// with a_rc = 2 Re H_rc, b_rc = -2 Im H_rc: about half the products of
+// forming M v.  complex128 groups are evaluated in double-float on the FP32
+// pipe, complex64 groups in FP32 (partial per group, then double-float).
+template <int K> struct HermArgs {
+    static constexpr int D = 1 << K, P = D * (D - 1) / 2;
+    Masks mk;
+    uint64_t ngroups;
+    uint64_t off[D];
+    float dh[D], dl[D];         // H_rr
+    float ah[P], al[P], bh[P], bl[P];
+};
+
+// the r < c pair terms of a complex128 group, unrolled at compile time
+template <int D, int R, int C, int K>
+__device__ __forceinline__ void herm_pairs_df(const CDF (&w)[D], const HermArgs<K> &a, DAcc &acc) {
+    if constexpr (R < D - 1) {
+        constexpr int P = R * D - R * (R + 1) / 2 + (C - R - 1); // index of (R, C) among r < c pairs
+        float xh, xl, yh, yl;
+        df_first(w[R].re.hi, w[R].re.lo, w[C].re.hi, w[C].re.lo, xh, xl);
+        df_mac(w[R].im.hi, w[R].im.lo, w[C].im.hi, w[C].im.lo, xh, xl);
+        df_first(w[R].re.hi, w[R].re.lo, w[C].im.hi, w[C].im.lo, yh, yl);
+        df_mac(-w[R].im.hi, -w[R].im.lo, w[C].re.hi, w[C].re.lo, yh, yl);
+        df_mac(a.ah[P], a.al[P], xh, xl, acc.h, acc.l);
+        df_mac(a.bh[P], a.bl[P], yh, yl, acc.h, acc.l);
+        if constexpr (C + 1 < D) herm_pairs_df<D, R, C + 1>(w, a, acc);
+        else herm_pairs_df<D, R + 1, R + 2>(w, a, acc);
+    }
+}
+
 template <class T, int K>
 __global__ void __launch_bounds__(kThreads)
-    k_expval_mat(const c2_t<T> *__restrict__ sv, Masks mk, uint64_t ngroups, const uint64_t off0, const uint64_t off1,
-                 const uint64_t off2, const uint64_t off3, const double2 *__restrict__ mat, double *partials,
-                 double *result, unsigned *counter) {
+    k_expval_herm(const c2_t<T> *__restrict__ sv, const HermArgs<K> a, double *partials, double *result,
+                  unsigned *counter) {
     constexpr int D = 1 << K;
-    __shared__ double2 m[D * D];
-    for (int i = threadIdx.x; i < D * D; i += blockDim.x) m[i] = mat[i];
-    __syncthreads();
-    const uint64_t off[4] = {off0, off1, off2, off3};
-    double acc[1] = {0.0};
+    constexpr int UG = K == 1 ? 4 : (K == 2 ? 2 : 1); // groups in flight per thread
+    DAcc acc;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ngroups; g += step) {
-        const uint64_t base = group_base<K>(g, mk);
-        double vr[D], vi[D];
+    for (uint64_t g0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g0 < a.ngroups; g0 += step * UG) {
+        c2_t<T> v[UG][D];
 #pragma unroll
-        for (int i = 0; i < D; i++) {
-            const c2_t<T> a = sv[base + off[i]];
-            vr[i] = a.x;
-            vi[i] = a.y;
+        for (int u = 0; u < UG; u++) {
+            const uint64_t g = g0 + u * step;
+            const uint64_t base = group_base<K>(g < a.ngroups ? g : 0, a.mk);
+#pragma unroll
+            for (int i = 0; i < D; i++) v[u][i] = g < a.ngroups ? sv[base + a.off[i]] : mk<c2_t<T>>(0, 0);
         }
 #pragma unroll
-        for (int r = 0; r < D; r++) {
-            double mr = 0.0, mi = 0.0;
+        for (int u = 0; u < UG; u++) {
+            if constexpr (sizeof(T) == 4) {
+                float t = 0.0f;
 #pragma unroll
-            for (int c = 0; c < D; c++) {
-                const double2 e = m[r * D + c];
-                mr += e.x * vr[c] - e.y * vi[c];
-                mi += e.x * vi[c] + e.y * vr[c];
+                for (int r = 0; r < D; r++) t = fmaf(a.dh[r], fmaf(v[u][r].x, v[u][r].x, v[u][r].y * v[u][r].y), t);
+                int p = 0;
+#pragma unroll
+                for (int r = 0; r < D; r++)
+#pragma unroll
+                    for (int c = r + 1; c < D; c++, p++) {
+                        const float x = fmaf(v[u][r].x, v[u][c].x, v[u][r].y * v[u][c].y);
+                        const float y = fmaf(v[u][r].x, v[u][c].y, -v[u][r].y * v[u][c].x);
+                        t = fmaf(a.ah[p], x, fmaf(a.bh[p], y, t));
+                    }
+                acc.add(DF{t, 0.0f});
+            } else {
+                CDF w[D];
+#pragma unroll
+                for (int i = 0; i < D; i++) w[i] = to_cdf(v[u][i]);
+#pragma unroll
+                for (int r = 0; r < D; r++) {
+                    const DF n = df_norm2(w[r]);
+                    df_mac(a.dh[r], a.dl[r], n.hi, n.lo, acc.h, acc.l);
+                }
+                herm_pairs_df<D, 0, 1>(w, a, acc);
             }
-            acc[0] += vr[r] * mr + vi[r] * mi; // Re(conj(v_r) (M v)_r)
         }
     }
-    block_reduce_finish<1>(acc, partials, result, counter);
+    double r[1] = {acc.value()};
+    block_reduce_finish<1>(r, partials, result, counter);
 }
 
 // <x|y> = sum conj(x_k) y_k -> (re, im)
@@ -295,82 +408,158 @@ static int build_pauli_groups(plk_state s, int nterms, const double *coeffs, con
 // (m, m ^ x) with bit p (the top bit of x) clear are visited once:
 //   conj(psi_m) psi_m' f(m') + conj(psi_m') psi_m f(m),
 //   f(q) = sum_t c_t i^ny (-1)^popcount(q & z_t).
+// contribution of the pair (m, mp = m ^ x) to <psi|sum c_t P_t|psi> (complex64:
+// formed in FP32, returned for a double-float add)
+__device__ __forceinline__ float pauli_pair_f32(float2 a, float2 b, uint64_t m, uint64_t mp,
+                                                const PauliTerm *__restrict__ st, int nt) {
+    float f1 = 0.0f, f2 = 0.0f;
+    for (int t = 0; t < nt; t++) {
+        const PauliTerm tt = st[t];
+        const bool s1 = __popcll(mp & tt.z) & 1, s0 = __popcll(m & tt.z) & 1;
+        if (s1 == s0) f1 += s0 ? -2.0f * tt.crh : 2.0f * tt.crh;
+        else f2 += s0 ? -2.0f * tt.cih : 2.0f * tt.cih;
+    }
+    const float re = fmaf(a.x, b.x, a.y * b.y), im = fmaf(a.x, b.y, -a.y * b.x);
+    return fmaf(re, f1, im * f2);
+}
+
+// complex128: the same in double-float, added to `total`
+__device__ __forceinline__ void pauli_pair_df(double2 ra, double2 rb, uint64_t m, uint64_t mp,
+                                              const PauliTerm *__restrict__ st, int nt, DAcc &total) {
+    const CDF a = to_cdf(ra), b = to_cdf(rb);
+    // F1 = Re f(m') + Re f(m), F2 = Im f(m) - Im f(m')
+    DAcc f1, f2;
+    for (int t = 0; t < nt; t++) {
+        const PauliTerm tt = st[t];
+        const bool s1 = __popcll(mp & tt.z) & 1, s0 = __popcll(m & tt.z) & 1;
+        if (s1 == s0) {
+            const DF c = {2.0f * tt.crh, 2.0f * tt.crl};
+            if (s0) f1.sub(c);
+            else f1.add(c);
+        } else {
+            const DF c = {2.0f * tt.cih, 2.0f * tt.cil};
+            if (s0) f2.sub(c); // s0 set: -ci from f(m), s1 clear: +ci from -f(m')
+            else f2.add(c);
+        }
+    }
+    DAcc ab_re, ab_im; // conj(a) b
+    ab_re.mac(a.re, b.re);
+    ab_re.mac(a.im, b.im);
+    ab_im.mac(a.re, b.im);
+    ab_im.msub(a.im, b.re);
+    total.mac(ab_re.normalized(), f1.normalized());
+    total.mac(ab_im.normalized(), f2.normalized());
+}
+
+__device__ __forceinline__ float pauli_diag_f32(float2 a, uint64_t k, const PauliTerm *__restrict__ st, int nt) {
+    float f = 0.0f;
+    for (int t = 0; t < nt; t++) f += (__popcll(k & st[t].z) & 1) ? -st[t].crh : st[t].crh;
+    return fmaf(a.x, a.x, a.y * a.y) * f;
+}
+
+__device__ __forceinline__ void pauli_diag_df(double2 ra, uint64_t k, const PauliTerm *__restrict__ st, int nt,
+                                              DAcc &total) {
+    const DF p = df_norm2(to_cdf(ra));
+    DAcc f;
+    for (int t = 0; t < nt; t++) {
+        const DF c = {st[t].crh, st[t].crl};
+        if (__popcll(k & st[t].z) & 1) f.sub(c);
+        else f.add(c);
+    }
+    total.mac(p, f.normalized());
+}
+
+// <psi| sum_{t in group} c_t P_t |psi> for one x-group.  For x != 0 the pairs
+// (m, m ^ x) with bit p (the top bit of x) clear are visited once:
+//   conj(psi_m) psi_m' f(m') + conj(psi_m') psi_m f(m),
+//   f(q) = sum_t c_t i^ny (-1)^popcount(q & z_t).
+// Software-pipelined: the loads of the next kPauliBatch items are issued
+// before the current batch is evaluated, so every thread keeps loads in
+// flight while it computes.
+constexpr int kPauliBatch = 4;
+
 template <class T>
 __global__ void __launch_bounds__(kThreads)
     k_expval_pauli(const c2_t<T> *__restrict__ sv, uint64_t n, uint64_t x, uint64_t pmask_lo,
                    const PauliTerm *__restrict__ terms, int nt, double *partials, double *result, unsigned *counter) {
+    using V = c2_t<T>;
+    constexpr int U = sizeof(T) == 8 ? kPauliBatch / 2 : kPauliBatch;
     extern __shared__ PauliTerm sterm[];
     for (int i = threadIdx.x; i < nt; i += blockDim.x) sterm[i] = terms[i];
     __syncthreads();
-    // coefficients of the group as double-floats (split once per thread)
     DAcc total;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    if constexpr (sizeof(T) == 4) {
-        // complex64: each amplitude (pair)'s contribution formed in FP32,
-        // accumulated in double-float
-        if (x == 0) {
-            for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
-                const float2 a = sv[k];
-                float f = 0.0f;
-                for (int t = 0; t < nt; t++) f += (__popcll(k & sterm[t].z) & 1) ? -sterm[t].crh : sterm[t].crh;
-                total.add(DF{fmaf(a.x, a.x, a.y * a.y) * f, 0.0f});
-            }
-        } else {
-            const uint64_t half = n >> 1;
-            for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < half; g += step) {
-                const uint64_t m = ((g & ~pmask_lo) << 1) | (g & pmask_lo);
-                const uint64_t mp = m ^ x;
-                const float2 a = sv[m], b = sv[mp];
-                float f1 = 0.0f, f2 = 0.0f;
-                for (int t = 0; t < nt; t++) {
-                    const PauliTerm tt = sterm[t];
-                    const bool s1 = __popcll(mp & tt.z) & 1, s0 = __popcll(m & tt.z) & 1;
-                    if (s1 == s0) f1 += s0 ? -2.0f * tt.crh : 2.0f * tt.crh;
-                    else f2 += s0 ? -2.0f * tt.cih : 2.0f * tt.cih;
-                }
-                const float re = fmaf(a.x, b.x, a.y * b.y), im = fmaf(a.x, b.y, -a.y * b.x);
-                total.add(DF{fmaf(re, f1, im * f2), 0.0f});
-            }
+    const uint64_t items = x == 0 ? n : (n >> 1);
+    const V zero = mk<V>(0, 0);
+    // One-term group with x != 0 (most Pauli words): the parities of m and
+    // m ^ x under z differ exactly when x & z has odd parity, so only
+    // Re(conj(a) b) (even) or only Im(conj(a) b) (odd) contributes, with
+    // coefficient 2 cr or 2 ci signed by the parity of m & z.  complex128
+    // forms that product of the pair in native FP64 (two FP64 instructions
+    // per pair, inside the FP64 pipe's budget at HBM speed) and accumulates
+    // it in double-float.
+    const bool single = nt == 1 && x != 0;
+    const uint64_t z1 = sterm[0].z;
+    const bool px = single && (__popcll(x & z1) & 1);
+    const float cf = px ? 2.0f * sterm[0].cih : 2.0f * sterm[0].crh;
+    const DF cd = px ? DF{2.0f * sterm[0].cih, 2.0f * sterm[0].cil} : DF{2.0f * sterm[0].crh, 2.0f * sterm[0].crl};
+    // item g -> (m, m ^ x); for x == 0, m = g
+    auto first_of = [&](uint64_t g) { return x == 0 ? g : (((g & ~pmask_lo) << 1) | (g & pmask_lo)); };
+    V a[U], b[U];
+    uint64_t g0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        const uint64_t g = g0 + u * step;
+        const uint64_t m = first_of(g);
+        a[u] = g < items ? sv[m] : zero;
+        b[u] = (x != 0 && g < items) ? sv[m ^ x] : zero;
+    }
+    for (; g0 < items; g0 += step * U) {
+        V na[U], nb[U];
+        const uint64_t g1 = g0 + step * U;
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const uint64_t g = g1 + u * step;
+            const uint64_t m = first_of(g);
+            na[u] = g < items ? sv[m] : zero;
+            nb[u] = (x != 0 && g < items) ? sv[m ^ x] : zero;
         }
-    } else if (x == 0) {
-        for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
-            const DF p = df_norm2(to_cdf(sv[k]));
-            DAcc f;
-            for (int t = 0; t < nt; t++) {
-                const DF c = {sterm[t].crh, sterm[t].crl};
-                if (__popcll(k & sterm[t].z) & 1) f.sub(c);
-                else f.add(c);
-            }
-            total.mac(p, f.normalized());
-        }
-    } else {
-        const uint64_t half = n >> 1;
-        for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < half; g += step) {
-            const uint64_t m = ((g & ~pmask_lo) << 1) | (g & pmask_lo);
-            const uint64_t mp = m ^ x;
-            const CDF a = to_cdf(sv[m]), b = to_cdf(sv[mp]);
-            // F1 = Re f(m') + Re f(m), F2 = Im f(m) - Im f(m')
-            DAcc f1, f2;
-            for (int t = 0; t < nt; t++) {
-                const PauliTerm tt = sterm[t];
-                const bool s1 = __popcll(mp & tt.z) & 1, s0 = __popcll(m & tt.z) & 1;
-                if (s1 == s0) {
-                    const DF c = {2.0f * tt.crh, 2.0f * tt.crl};
-                    if (s0) f1.sub(c);
-                    else f1.add(c);
+        if (single) {
+            // items past the end hold zero amplitudes: they add nothing
+            float t = 0.0f;
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const uint64_t m = first_of(g0 + u * step);
+                const bool neg = __popcll(m & z1) & 1;
+                if constexpr (sizeof(T) == 4) {
+                    const float v = px ? fmaf(a[u].x, b[u].y, -a[u].y * b[u].x) : fmaf(a[u].x, b[u].x, a[u].y * b[u].y);
+                    t = fmaf(neg ? -cf : cf, v, t);
                 } else {
-                    const DF c = {2.0f * tt.cih, 2.0f * tt.cil};
-                    if (s0) f2.sub(c); // s0 set: -ci from f(m), s1 clear: +ci from -f(m')
-                    else f2.add(c);
+                    const double v = px ? fma(a[u].x, b[u].y, -a[u].y * b[u].x) : fma(a[u].x, b[u].x, a[u].y * b[u].y);
+                    total.mac(neg ? DF{-cd.hi, -cd.lo} : cd, df_split(v));
                 }
             }
-            DAcc ab_re, ab_im; // conj(a) b
-            ab_re.mac(a.re, b.re);
-            ab_re.mac(a.im, b.im);
-            ab_im.mac(a.re, b.im);
-            ab_im.msub(a.im, b.re);
-            total.mac(ab_re.normalized(), f1.normalized());
-            total.mac(ab_im.normalized(), f2.normalized());
+            if constexpr (sizeof(T) == 4) total.add(DF{t, 0.0f});
+        } else {
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const uint64_t g = g0 + u * step;
+                if (g >= items) break;
+                const uint64_t m = first_of(g);
+                if constexpr (sizeof(T) == 4) {
+                    const float c = x == 0 ? pauli_diag_f32(a[u], m, sterm, nt)
+                                           : pauli_pair_f32(a[u], b[u], m, m ^ x, sterm, nt);
+                    total.add(DF{c, 0.0f});
+                } else {
+                    if (x == 0) pauli_diag_df(a[u], m, sterm, nt, total);
+                    else pauli_pair_df(a[u], b[u], m, m ^ x, sterm, nt, total);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            a[u] = na[u];
+            b[u] = nb[u];
         }
     }
     double acc[1] = {total.value()};
@@ -378,7 +567,7 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // out_m (+)= sum_{groups g} sum_{t in g} c_t i^ny (-1)^popcount((m^x_g) & z_t) in_{m ^ x_g}
-constexpr int kPauliGroupsPerPass = 8;
+constexpr int kPauliGroupsPerPass = 32;
 struct PauliPass {
     uint64_t x[kPauliGroupsPerPass];
     int first[kPauliGroupsPerPass];
@@ -391,62 +580,153 @@ struct PauliPass {
 // f_g(src) = sum_t c_t i^ny_t (-1)^popc(src & z_t).  complex64 states in FP32
 // (the result is stored in FP32); complex128 on the FP32 pipe in
 // double-float, rounded once to FP64.
+// f_g(src) = sum over the group's terms of c_t i^ny (-1)^popc(src & z_t), as
+// double-floats; a one-term group needs no accumulation
+__device__ __forceinline__ void pauli_coef_df(const PauliTerm *__restrict__ tp, int first, int count, uint64_t src,
+                                              DF &f_re, DF &f_im) {
+    if (count == 1) {
+        const PauliTerm &tt = tp[first];
+        const bool neg = __popcll(src & tt.z) & 1;
+        f_re = neg ? DF{-tt.crh, -tt.crl} : DF{tt.crh, tt.crl};
+        f_im = neg ? DF{-tt.cih, -tt.cil} : DF{tt.cih, tt.cil};
+        return;
+    }
+    DAcc fr, fi;
+    for (int t = first; t < first + count; t++) {
+        const PauliTerm &tt = tp[t];
+        if (__popcll(src & tt.z) & 1) {
+            fr.sub(DF{tt.crh, tt.crl});
+            fi.sub(DF{tt.cih, tt.cil});
+        } else {
+            fr.add(DF{tt.crh, tt.crl});
+            fi.add(DF{tt.cih, tt.cil});
+        }
+    }
+    f_re = fr.normalized();
+    f_im = fi.normalized();
+}
+
+// out[m] (+)= sum over groups g of f_g(src) in[src], src = m ^ x_g.  complex64
+// states in FP32 (the result is stored in FP32); complex128 on the FP32 pipe
+// in double-float.  The pass's terms sit in shared memory (tp = sterm, term
+// indices relative to t_lo) when they fit, else are read from global memory.
+// A block owns a tile of 2048 consecutive outputs (8 per thread, kept in
+// registers) and walks the groups in order: for each group the block reads
+// one contiguous source tile (the output tile with x's high bits flipped,
+// permuted inside by x's low bits), with eight loads in flight per thread.
+constexpr int kPauliPerThread = 8;
+constexpr int kPauliTile = kThreads * kPauliPerThread;
+
 template <class T>
 __global__ void __launch_bounds__(kThreads)
     k_apply_pauli(c2_t<T> *__restrict__ out, const c2_t<T> *__restrict__ in, uint64_t n,
-                  const PauliTerm *__restrict__ terms, const PauliPass pass) {
-    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t m = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; m < n; m += step) {
-        if constexpr (sizeof(T) == 4) {
-            float ar = 0.0f, ai = 0.0f;
-            if (pass.accumulate) {
-                const float2 o = out[m];
-                ar = o.x;
-                ai = o.y;
+                  const PauliTerm *__restrict__ terms, const PauliPass pass, int t_lo, int t_cnt, int terms_in_smem) {
+    using V = c2_t<T>;
+    constexpr int P = kPauliPerThread;
+    extern __shared__ PauliTerm sterm[];
+    if (terms_in_smem) {
+        for (int i = threadIdx.x; i < t_cnt; i += blockDim.x) sterm[i] = terms[t_lo + i];
+        __syncthreads();
+    }
+    const PauliTerm *tp = terms_in_smem ? sterm : terms + t_lo;
+    const int ng = pass.ngroups;
+    const uint64_t ntiles = (n + kPauliTile - 1) / kPauliTile;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t m0 = tile * kPauliTile + threadIdx.x;
+        // accumulators: complex64 in FP32, complex128 in double-float
+        float ar[P], ai[P];
+        DAcc dr[P], di[P];
+#pragma unroll
+        for (int i = 0; i < P; i++) {
+            const uint64_t m = m0 + (uint64_t)i * kThreads;
+            const V o = (pass.accumulate && m < n) ? out[m] : mk<V>(0, 0);
+            if constexpr (sizeof(T) == 4) {
+                ar[i] = o.x;
+                ai[i] = o.y;
+            } else {
+                const CDF oc = to_cdf(o);
+                dr[i].add(oc.re);
+                di[i].add(oc.im);
             }
-            for (int gi = 0; gi < pass.ngroups; gi++) {
-                const uint64_t src = m ^ pass.x[gi];
-                const float2 v = in[src];
-                float fr = 0.0f, fi = 0.0f;
-                for (int t = pass.first[gi]; t < pass.first[gi] + pass.count[gi]; t++) {
-                    const PauliTerm tt = terms[t];
-                    const bool neg = __popcll(src & tt.z) & 1;
-                    fr += neg ? -tt.crh : tt.crh;
-                    fi += neg ? -tt.cih : tt.cih;
-                }
-                ar = fmaf(fr, v.x, fmaf(-fi, v.y, ar));
-                ai = fmaf(fr, v.y, fmaf(fi, v.x, ai));
+        }
+        for (int gi = 0; gi < ng; gi++) {
+            const uint64_t x = pass.x[gi];
+            // m0 has bits 8-10 clear, so source i is (m0 ^ x) ^ (i << 8)
+            const uint64_t y = m0 ^ x;
+            V v[P];
+#pragma unroll
+            for (int i = 0; i < P; i++) {
+                const uint64_t m = m0 + (uint64_t)i * kThreads;
+                v[i] = m < n ? in[y ^ ((uint64_t)i << 8)] : mk<V>(0, 0);
             }
-            out[m] = make_float2(ar, ai);
-        } else {
-            DAcc ar, ai;
-            if (pass.accumulate) {
-                const CDF o = to_cdf(out[m]);
-                ar.add(o.re);
-                ai.add(o.im);
-            }
-            for (int gi = 0; gi < pass.ngroups; gi++) {
-                const uint64_t src = m ^ pass.x[gi];
-                const CDF v = to_cdf(in[src]);
-                DAcc fr, fi;
-                for (int t = pass.first[gi]; t < pass.first[gi] + pass.count[gi]; t++) {
-                    const PauliTerm tt = terms[t];
-                    const bool neg = __popcll(src & tt.z) & 1;
-                    if (neg) {
-                        fr.sub(DF{tt.crh, tt.crl});
-                        fi.sub(DF{tt.cih, tt.cil});
+            const int first = pass.first[gi] - t_lo, count = pass.count[gi];
+            const bool one_term = count == 1 && ((tp[first].cih == 0.0f && tp[first].cil == 0.0f) ||
+                                                 (tp[first].crh == 0.0f && tp[first].crl == 0.0f));
+            if (one_term) {
+                // one term: f = (-1)^popcount(src & z) c with c real or
+                // imaginary; popcount(src & z) = popcount(y & z) + that of
+                // (i << 8) & z
+                const PauliTerm &tt = tp[first];
+                const uint32_t zi = (uint32_t)(tt.z >> 8) & 7u;
+                const bool py = __popcll(y & tt.z) & 1;
+                const bool is_real = tt.cih == 0.0f && tt.cil == 0.0f;
+#pragma unroll
+                for (int i = 0; i < P; i++) {
+                    const bool neg = py ^ (__popc((uint32_t)i & zi) & 1);
+                    if constexpr (sizeof(T) == 4) {
+                        const float c = is_real ? tt.crh : tt.cih;
+                        const float cs = neg ? -c : c;
+                        if (is_real) {
+                            ar[i] = fmaf(cs, v[i].x, ar[i]);
+                            ai[i] = fmaf(cs, v[i].y, ai[i]);
+                        } else { // i c v: (-c v.y, c v.x)
+                            ar[i] = fmaf(-cs, v[i].y, ar[i]);
+                            ai[i] = fmaf(cs, v[i].x, ai[i]);
+                        }
                     } else {
-                        fr.add(DF{tt.crh, tt.crl});
-                        fi.add(DF{tt.cih, tt.cil});
+                        const CDF c = to_cdf(v[i]);
+                        const DF k = is_real ? DF{tt.crh, tt.crl} : DF{tt.cih, tt.cil};
+                        const DF ks = neg ? DF{-k.hi, -k.lo} : k;
+                        if (is_real) {
+                            dr[i].mac(ks, c.re);
+                            di[i].mac(ks, c.im);
+                        } else {
+                            dr[i].msub(ks, c.im);
+                            di[i].mac(ks, c.re);
+                        }
                     }
                 }
-                const DF f_re = fr.normalized(), f_im = fi.normalized();
-                ar.mac(f_re, v.re);
-                ar.msub(f_im, v.im);
-                ai.mac(f_re, v.im);
-                ai.mac(f_im, v.re);
+                continue;
             }
-            out[m] = make_double2(ar.value(), ai.value());
+#pragma unroll
+            for (int i = 0; i < P; i++) {
+                const uint64_t src = (m0 + (uint64_t)i * kThreads) ^ x;
+                if constexpr (sizeof(T) == 4) {
+                    float fr = 0.0f, fi = 0.0f;
+                    for (int t = first; t < first + count; t++) {
+                        const bool neg = __popcll(src & tp[t].z) & 1;
+                        fr += neg ? -tp[t].crh : tp[t].crh;
+                        fi += neg ? -tp[t].cih : tp[t].cih;
+                    }
+                    ar[i] = fmaf(fr, v[i].x, fmaf(-fi, v[i].y, ar[i]));
+                    ai[i] = fmaf(fr, v[i].y, fmaf(fi, v[i].x, ai[i]));
+                } else {
+                    const CDF c = to_cdf(v[i]);
+                    DF f_re, f_im;
+                    pauli_coef_df(tp, first, count, src, f_re, f_im);
+                    dr[i].mac(f_re, c.re);
+                    dr[i].msub(f_im, c.im);
+                    di[i].mac(f_re, c.im);
+                    di[i].mac(f_im, c.re);
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < P; i++) {
+            const uint64_t m = m0 + (uint64_t)i * kThreads;
+            if (m >= n) continue;
+            if constexpr (sizeof(T) == 4) out[m] = make_float2(ar[i], ai[i]);
+            else out[m] = make_double2(dr[i].value(), di[i].value());
         }
     }
 }
@@ -476,64 +756,75 @@ static int expval_named_impl(plk_state s, int gate, int64_t wire, double *out) {
     return fetch_results(s, 1, out);
 }
 
-template <class T, int NV> static void launch_diag(plk_state s, int grid, const uint64_t *dz, int nv) {
+template <class T, int NV> static void launch_diag(plk_state s, const DiagMasks &dm, int nv) {
     auto &w = s->ws;
-    k_expval_diag<T, NV><<<grid, kThreads, 0, s->stream>>>((const c2_t<T> *)s->data, s->length, dz, nv, w.d_partials,
+    const int grid = red_grid_k(s, k_expval_diag<T, NV>, ((s->length + 127) >> 7) << 5);
+    k_expval_diag<T, NV><<<grid, kThreads, 0, s->stream>>>((const c2_t<T> *)s->data, s->length, dm, nv, w.d_partials,
                                                           w.d_result, w.d_counter);
 }
 
 // Diagonal (Identity / PauliZ) observables, up to 16 per pass.
 template <class T> static int expval_diag_impl(plk_state s, const std::vector<uint64_t> &zmasks, double *out) {
     const int total = (int)zmasks.size();
-    uint64_t *dz = nullptr;
-    PLK_CUDA(cudaMallocAsync((void **)&dz, sizeof(uint64_t) * std::max(total, 1), s->stream));
-    PLK_CUDA(cudaMemcpyAsync(dz, zmasks.data(), sizeof(uint64_t) * total, cudaMemcpyHostToDevice, s->stream));
-    const int grid = red_grid(s, s->length);
     for (int start = 0; start < total; start += 16) {
         const int nv = std::min(16, total - start);
-        if (nv == 1) launch_diag<T, 1>(s, grid, dz + start, nv);
-        else if (nv == 2) launch_diag<T, 2>(s, grid, dz + start, nv);
-        else if (nv <= 4) launch_diag<T, 4>(s, grid, dz + start, nv);
-        else if (nv <= 8) launch_diag<T, 8>(s, grid, dz + start, nv);
-        else launch_diag<T, 16>(s, grid, dz + start, nv);
+        DiagMasks dm{};
+        for (int v = 0; v < nv; v++) dm.z[v] = zmasks[start + v];
+        if (nv == 1) launch_diag<T, 1>(s, dm, nv);
+        else if (nv == 2) launch_diag<T, 2>(s, dm, nv);
+        else if (nv <= 4) launch_diag<T, 4>(s, dm, nv);
+        else if (nv <= 8) launch_diag<T, 8>(s, dm, nv);
+        else launch_diag<T, 16>(s, dm, nv);
         PLK_CHECK_LAUNCH();
         PLK_TRY(fetch_results(s, nv, out + start));
     }
-    PLK_CUDA(cudaFreeAsync(dz, s->stream));
     return PLK_OK;
 }
 
-template <class T>
-static int expval_mat12_impl(plk_state s, const double *matrix, const int64_t *wires, int K, double *out) {
-    int rev[2], srt[2];
+template <class T, int K>
+static int expval_herm_impl(plk_state s, const double *matrix, const int64_t *wires, double *out) {
+    constexpr int D = 1 << K;
+    HermArgs<K> a;
+    std::memset(&a, 0, sizeof(a));
+    int rev[K], srt[K];
     for (int j = 0; j < K; j++) rev[j] = s->nq - 1 - (int)wires[j];
     std::copy(rev, rev + K, srt);
     std::sort(srt, srt + K);
-    const Masks mk = make_masks(srt, K);
-    uint64_t off[4] = {0, 0, 0, 0};
-    for (int i = 0; i < (1 << K); i++)
+    a.mk = make_masks(srt, K);
+    a.ngroups = s->length >> K;
+    for (int i = 0; i < D; i++)
         for (int j = 0; j < K; j++)
-            if ((i >> (K - 1 - j)) & 1) off[i] |= 1ULL << rev[j];
-    const int D = 1 << K;
-    double2 *dm = nullptr;
-    PLK_CUDA(cudaMallocAsync((void **)&dm, sizeof(double2) * D * D, s->stream));
-    PLK_CUDA(cudaMemcpyAsync(dm, matrix, sizeof(double2) * D * D, cudaMemcpyHostToDevice, s->stream));
-    const uint64_t ng = s->length >> K;
-    const int grid = red_grid(s, ng);
+            if ((i >> (K - 1 - j)) & 1) a.off[i] |= 1ULL << rev[j];
+    // Hermitian part H = (M + M^dag)/2 of the row-major complex matrix
+    auto re = [&](int r, int c) { return matrix[2 * (r * D + c)]; };
+    auto im = [&](int r, int c) { return matrix[2 * (r * D + c) + 1]; };
+    for (int r = 0; r < D; r++) df_split_host(re(r, r), a.dh[r], a.dl[r]);
+    int p = 0;
+    for (int r = 0; r < D; r++)
+        for (int c = r + 1; c < D; c++, p++) {
+            const double hre = 0.5 * (re(r, c) + re(c, r)), him = 0.5 * (im(r, c) - im(c, r));
+            df_split_host(2.0 * hre, a.ah[p], a.al[p]);
+            df_split_host(-2.0 * him, a.bh[p], a.bl[p]);
+        }
+    const int grid = red_grid_k(s, k_expval_herm<T, K>, a.ngroups);
     auto &w = s->ws;
-    if (K == 1)
-        k_expval_mat<T, 1><<<grid, kThreads, 0, s->stream>>>((const c2_t<T> *)s->data, mk, ng, off[0], off[1], 0, 0, dm,
-                                                             w.d_partials, w.d_result, w.d_counter);
-    else
-        k_expval_mat<T, 2><<<grid, kThreads, 0, s->stream>>>((const c2_t<T> *)s->data, mk, ng, off[0], off[1], off[2],
-                                                             off[3], dm, w.d_partials, w.d_result, w.d_counter);
+    k_expval_herm<T, K><<<grid, kThreads, 0, s->stream>>>((const c2_t<T> *)s->data, a, w.d_partials, w.d_result,
+                                                          w.d_counter);
     PLK_CHECK_LAUNCH();
-    PLK_CUDA(cudaFreeAsync(dm, s->stream));
     return fetch_results(s, 1, out);
 }
 
+template <class T> static int expval_herm_any(plk_state s, const double *matrix, const int64_t *wires, int K,
+                                              double *out) {
+    switch (K) {
+    case 1: return expval_herm_impl<T, 1>(s, matrix, wires, out);
+    case 2: return expval_herm_impl<T, 2>(s, matrix, wires, out);
+    default: return expval_herm_impl<T, 3>(s, matrix, wires, out);
+    }
+}
+
 template <class T> static int inner_impl(plk_state x, plk_state y, double *re, double *im) {
-    const int grid = red_grid(x, x->length);
+    const int grid = red_grid_k(x, k_inner<T>, x->length);
     auto &w = x->ws;
     k_inner<T><<<grid, kThreads, 0, x->stream>>>((const c2_t<T> *)x->data, (const c2_t<T> *)y->data, x->length,
                                                  w.d_partials, w.d_result, w.d_counter);
@@ -581,12 +872,12 @@ static int free_csr(plk_state s, CsrDev &c) {
 template <class T>
 static int pauli_expval_impl(plk_state s, const std::vector<PauliGroup> &groups, const std::vector<PauliTerm> &terms,
                              double *out) {
-    PauliTerm *dt = nullptr;
-    PLK_CUDA(cudaMallocAsync((void **)&dt, sizeof(PauliTerm) * std::max<size_t>(terms.size(), 1), s->stream));
+    PoolBuf dt_buf(s->stream);
+    PLK_TRY(pool_alloc(s->device, &dt_buf.p, sizeof(PauliTerm) * std::max<size_t>(terms.size(), 1), s->stream));
+    PauliTerm *dt = dt_buf.as<PauliTerm>();
     PLK_CUDA(cudaMemcpyAsync(dt, terms.data(), sizeof(PauliTerm) * terms.size(), cudaMemcpyHostToDevice, s->stream));
     // each group's partial lands in d_result[gi % kMaxRedValues]; fetch in chunks
     double total = 0.0;
-    const int grid = red_grid(s, s->length);
     auto &w = s->ws;
     std::vector<double> vals(groups.size());
     for (size_t gi = 0; gi < groups.size(); gi++) {
@@ -598,6 +889,7 @@ static int pauli_expval_impl(plk_state s, const std::vector<PauliGroup> &groups,
         }
         const size_t smem = sizeof(PauliTerm) * g.count;
         if (smem > 48 * 1024) PLK_FAIL(PLK_ERR_UNSUPPORTED, "too many Pauli terms share one X pattern");
+        const int grid = red_grid_k(s, k_expval_pauli<T>, g.x ? s->length >> 1 : s->length, smem);
         k_expval_pauli<T><<<grid, kThreads, smem, s->stream>>>((const c2_t<T> *)s->data, s->length, g.x, pmask_lo,
                                                               dt + g.first, g.count, w.d_partials,
                                                               w.d_result + (gi % kMaxRedValues), w.d_counter);
@@ -608,7 +900,6 @@ static int pauli_expval_impl(plk_state s, const std::vector<PauliGroup> &groups,
         }
     }
     for (double v : vals) total += v; // fixed (group) order
-    PLK_CUDA(cudaFreeAsync(dt, s->stream));
     *out = total;
     return PLK_OK;
 }
@@ -616,11 +907,11 @@ static int pauli_expval_impl(plk_state s, const std::vector<PauliGroup> &groups,
 template <class T>
 static int pauli_apply_impl(plk_state outs, plk_state ins, const std::vector<PauliGroup> &groups,
                             const std::vector<PauliTerm> &terms) {
-    PauliTerm *dt = nullptr;
     cudaStream_t st = outs->stream;
-    PLK_CUDA(cudaMallocAsync((void **)&dt, sizeof(PauliTerm) * std::max<size_t>(terms.size(), 1), st));
+    PoolBuf dt_buf(st);
+    PLK_TRY(pool_alloc(outs->device, &dt_buf.p, sizeof(PauliTerm) * std::max<size_t>(terms.size(), 1), st));
+    PauliTerm *dt = dt_buf.as<PauliTerm>();
     PLK_CUDA(cudaMemcpyAsync(dt, terms.data(), sizeof(PauliTerm) * terms.size(), cudaMemcpyHostToDevice, st));
-    const int grid = elem_grid(outs, outs->length);
     if (groups.empty()) PLK_CUDA(cudaMemsetAsync(outs->data, 0, outs->length * amp_bytes(outs->dtype), st));
     for (size_t g0 = 0; g0 < groups.size(); g0 += kPauliGroupsPerPass) {
         PauliPass pass;
@@ -631,11 +922,25 @@ static int pauli_apply_impl(plk_state outs, plk_state ins, const std::vector<Pau
             pass.first[i] = groups[g0 + i].first;
             pass.count[i] = groups[g0 + i].count;
         }
-        k_apply_pauli<T><<<grid, kThreads, 0, st>>>((c2_t<T> *)outs->data, (const c2_t<T> *)ins->data, outs->length, dt,
-                                                    pass);
+        const int t_lo = pass.first[0];
+        const int t_cnt = pass.first[pass.ngroups - 1] + pass.count[pass.ngroups - 1] - t_lo;
+        const size_t smem = sizeof(PauliTerm) * (size_t)t_cnt;
+        const int in_smem = smem <= 48 * 1024 ? 1 : 0;
+        // one resident wave of blocks, each walking its tiles in order
+        int occ = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_apply_pauli<T>, kThreads, in_smem ? smem : 0) !=
+                cudaSuccess ||
+            occ < 1) {
+            cudaGetLastError();
+            occ = 1;
+        }
+        const int grid = (int)std::max<uint64_t>(
+            1, std::min<uint64_t>((outs->length + kPauliTile - 1) / kPauliTile,
+                                  (uint64_t)device_sm_count(outs->device) * occ));
+        k_apply_pauli<T><<<grid, kThreads, in_smem ? smem : 0, st>>>((c2_t<T> *)outs->data, (const c2_t<T> *)ins->data,
+                                                                     outs->length, dt, pass, t_lo, t_cnt, in_smem);
         PLK_CHECK_LAUNCH();
     }
-    PLK_CUDA(cudaFreeAsync(dt, st));
     PLK_CUDA(cudaStreamSynchronize(st)); // host term vectors go away on return
     return PLK_OK;
 }
@@ -709,10 +1014,10 @@ PLK_API int plk_expval_matrix(plk_state s, const double *matrix, const int64_t *
     if (nw < 1) PLK_FAIL(PLK_ERR_INVALID_ARG, "matrix observable needs wires");
     PLK_TRY(check_wires(s, wires, nw));
     PLK_CUDA(cudaSetDevice(s->device));
-    if (nw <= 2)
-        return s->dtype == PLK_C64 ? expval_mat12_impl<float>(s, matrix, wires, nw, out)
-                                   : expval_mat12_impl<double>(s, matrix, wires, nw, out);
-    // k >= 3: copy, apply, Re<psi|M psi> (MeasuresKokkos.hpp:339-345)
+    if (nw <= 3)
+        return s->dtype == PLK_C64 ? expval_herm_any<float>(s, matrix, wires, nw, out)
+                                   : expval_herm_any<double>(s, matrix, wires, nw, out);
+    // k >= 4: copy, apply, Re<psi|M psi> (MeasuresKokkos.hpp:339-345)
     plk_state tmp = nullptr;
     PLK_TRY(plk_state_create(s->nq, s->dtype, s->device, &tmp));
     int st = plk_state_set_stream(tmp, s->stream);

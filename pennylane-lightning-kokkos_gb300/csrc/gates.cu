@@ -373,20 +373,120 @@ __global__ void __launch_bounds__(kThreads) k_quad(c2_t<T> *__restrict__ sv, con
     }
 }
 
+// MultiRZ: element-wise parity phase, four amplitudes in flight per thread
+constexpr int kMrzUnroll = 4;
+
 template <class T, bool GEN>
 __global__ void __launch_bounds__(kThreads) k_mrz(c2_t<T> *__restrict__ sv, uint64_t n, uint64_t mask, T e0r, T e0i,
                                                    T e1r, T e1i) {
     using V = c2_t<T>;
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
-        const bool odd = __popcll(k & mask) & 1;
-        V v = sv[k];
-        if (GEN) {
-            if (odd) v = cneg(v);
-        } else {
-            v = odd ? cmul(v, mk<V>(e1r, e1i)) : cmul(v, mk<V>(e0r, e0i));
+    for (uint64_t k0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += step * kMrzUnroll) {
+        V v[kMrzUnroll];
+#pragma unroll
+        for (int u = 0; u < kMrzUnroll; u++)
+            if (k0 + u * step < n) v[u] = sv[k0 + u * step];
+#pragma unroll
+        for (int u = 0; u < kMrzUnroll; u++) {
+            const uint64_t k = k0 + u * step;
+            if (k >= n) break;
+            const bool odd = __popcll(k & mask) & 1;
+            if (GEN) {
+                if (odd) v[u] = cneg(v[u]);
+            } else {
+                v[u] = odd ? cmul(v[u], mk<V>(e1r, e1i)) : cmul(v[u], mk<V>(e0r, e0i));
+            }
+            sv[k] = v[u];
         }
-        sv[k] = v;
+    }
+}
+
+// complex128 MultiRZ with the phase products in double-float on the FP32
+// pipe: eh/el hold e0 (even parity) then e1 (odd parity), split hi/lo
+__global__ void __launch_bounds__(kThreads) k_mrz_df(double2 *__restrict__ sv, uint64_t n, uint64_t mask,
+                                                      const float4 eh, const float4 el) {
+    const float h0[2] = {eh.x, eh.y}, h1[2] = {eh.z, eh.w};
+    const float l0[2] = {el.x, el.y}, l1[2] = {el.z, el.w};
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t k0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += step * kMrzUnroll) {
+        double2 v[kMrzUnroll];
+#pragma unroll
+        for (int u = 0; u < kMrzUnroll; u++)
+            if (k0 + u * step < n) v[u] = sv[k0 + u * step];
+#pragma unroll
+        for (int u = 0; u < kMrzUnroll; u++) {
+            const uint64_t k = k0 + u * step;
+            if (k >= n) break;
+            const bool odd = __popcll(k & mask) & 1;
+            // select the phase first: one product per amplitude
+            const float eh2[2] = {odd ? h1[0] : h0[0], odd ? h1[1] : h0[1]};
+            const float el2[2] = {odd ? l1[0] : l0[0], odd ? l1[1] : l0[1]};
+            sv[k] = df_cmul(eh2, el2, cdf_split(v[u]));
+        }
+    }
+}
+
+// Dense 2^K x 2^K matrix, K = 3 or 4: one thread per group, the group's
+// amplitudes in registers, the matrix in shared memory (read as broadcasts).
+// complex128 products run in double-float on the FP32 pipe (matrix split
+// into hi/lo floats: re.hi, re.lo, im.hi, im.lo per entry).
+template <int K> struct DenseRegArgs {
+    Masks mk;
+    uint64_t ngroups;
+    uint64_t off[1 << K];
+};
+
+template <class T, int K>
+__global__ void __launch_bounds__(kThreads)
+    k_dense_reg(c2_t<T> *__restrict__ sv, const DenseRegArgs<K> a, const float4 *__restrict__ mat_df,
+                const float2 *__restrict__ mat_f) {
+    constexpr int D = 1 << K;
+    using V = c2_t<T>;
+    __shared__ __align__(16) float4 m4[sizeof(T) == 8 ? D * D : 1];
+    __shared__ __align__(8) float2 m2[sizeof(T) == 8 ? 1 : D * D];
+    for (int i = threadIdx.x; i < D * D; i += blockDim.x) {
+        if constexpr (sizeof(T) == 8) m4[i] = mat_df[i];
+        else m2[i] = mat_f[i];
+    }
+    __syncthreads();
+    // one group per thread and no loop: a grid-stride loop would let the
+    // compiler hoist all D*D matrix reads out of it into registers
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g < a.ngroups) {
+        const uint64_t base = group_base<K>(g, a.mk);
+        V v[D];
+#pragma unroll
+        for (int i = 0; i < D; i++) v[i] = sv[base + a.off[i]];
+        if constexpr (sizeof(T) == 8) {
+            CDF w[D];
+#pragma unroll
+            for (int i = 0; i < D; i++) w[i] = cdf_split(v[i]);
+#pragma unroll
+            for (int r = 0; r < D; r++) {
+                float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
+#pragma unroll
+                for (int c = 0; c < D; c++) {
+                    const float4 e = m4[r * D + c];
+                    df_mac(e.x, e.y, w[c].re.hi, w[c].re.lo, rh, rl);
+                    df_mac(-e.z, -e.w, w[c].im.hi, w[c].im.lo, rh, rl);
+                    df_mac(e.x, e.y, w[c].im.hi, w[c].im.lo, ih, il);
+                    df_mac(e.z, e.w, w[c].re.hi, w[c].re.lo, ih, il);
+                }
+                sv[base + a.off[r]] = make_double2(df_result(rh, rl), df_result(ih, il));
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < D; r++) {
+                float re = 0.0f, im = 0.0f;
+#pragma unroll
+                for (int c = 0; c < D; c++) {
+                    const float2 e = m2[r * D + c];
+                    re = fmaf(e.x, v[c].x, fmaf(-e.y, v[c].y, re));
+                    im = fmaf(e.x, v[c].y, fmaf(e.y, v[c].x, im));
+                }
+                sv[base + a.off[r]] = make_float2(re, im);
+            }
+        }
     }
 }
 
@@ -558,7 +658,8 @@ int run_plan(plk_state s, const GatePlan &p, const int64_t *wires) {
     if (p.family == GatePlan::F_MRZ || p.family == GatePlan::F_GEN_MRZ) {
         uint64_t mask = 0;
         for (int j = 0; j < p.K; j++) mask |= 1ULL << (s->nq - 1 - (int)wires[j]);
-        const int grid = s->dtype == PLK_C64 ? gate_grid<float>(s, s->length, 1) : gate_grid<double>(s, s->length, 1);
+        const int grid = s->dtype == PLK_C64 ? gate_grid<float>(s, s->length, kMrzUnroll)
+                                             : gate_grid<double>(s, s->length, kMrzUnroll);
         const bool gen = p.family == GatePlan::F_GEN_MRZ;
         if (s->dtype == PLK_C64) {
             if (gen) k_mrz<float, true><<<grid, kThreads, 0, s->stream>>>((float2 *)s->data, s->length, mask, 0, 0, 0, 0);
@@ -567,8 +668,16 @@ int run_plan(plk_state s, const GatePlan &p, const int64_t *wires) {
                                                                        (float)p.coef[2], (float)p.coef[3]);
         } else {
             if (gen) k_mrz<double, true><<<grid, kThreads, 0, s->stream>>>((double2 *)s->data, s->length, mask, 0, 0, 0, 0);
-            else k_mrz<double, false><<<grid, kThreads, 0, s->stream>>>((double2 *)s->data, s->length, mask, p.coef[0],
-                                                                        p.coef[1], p.coef[2], p.coef[3]);
+            else if (c128_use_df()) {
+                float4 eh, el;
+                df_split_host(p.coef[0], eh.x, el.x);
+                df_split_host(p.coef[1], eh.y, el.y);
+                df_split_host(p.coef[2], eh.z, el.z);
+                df_split_host(p.coef[3], eh.w, el.w);
+                k_mrz_df<<<grid, kThreads, 0, s->stream>>>((double2 *)s->data, s->length, mask, eh, el);
+            } else
+                k_mrz<double, false><<<grid, kThreads, 0, s->stream>>>((double2 *)s->data, s->length, mask, p.coef[0],
+                                                                       p.coef[1], p.coef[2], p.coef[3]);
         }
         PLK_CHECK_LAUNCH();
         return PLK_OK;
@@ -579,6 +688,46 @@ int run_plan(plk_state s, const GatePlan &p, const int64_t *wires) {
     if (p.family == GatePlan::F_QUAD)
         return s->dtype == PLK_C64 ? run_quad<float>(s, p, g) : run_quad<double>(s, p, g);
     PLK_FAIL(PLK_ERR_UNSUPPORTED, "internal: bad plan family");
+}
+
+template <class T, int K>
+static int launch_dense_reg(plk_state s, const std::vector<c2_t<T>> &hm, const WireGeom &g) {
+    constexpr int D = 1 << K;
+    DenseRegArgs<K> a;
+    a.mk = g.mk;
+    a.ngroups = s->length >> K;
+    for (int i = 0; i < D; i++) a.off[i] = g.local_off(i);
+    std::vector<float4> mdf(sizeof(T) == 8 ? D * D : 0);
+    std::vector<float2> mf(sizeof(T) == 8 ? 0 : D * D);
+    for (int i = 0; i < D * D; i++) {
+        if constexpr (sizeof(T) == 8) {
+            df_split_host(hm[i].x, mdf[i].x, mdf[i].y);
+            df_split_host(hm[i].y, mdf[i].z, mdf[i].w);
+        } else {
+            mf[i] = make_float2((float)hm[i].x, (float)hm[i].y);
+        }
+    }
+    const size_t bytes = sizeof(T) == 8 ? sizeof(float4) * D * D : sizeof(float2) * D * D;
+    void *d_mat = nullptr;
+    PLK_TRY(pool_alloc(s->device, &d_mat, bytes, s->stream));
+    cudaError_t e = cudaMemcpyAsync(d_mat, sizeof(T) == 8 ? (const void *)mdf.data() : (const void *)mf.data(), bytes,
+                                    cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) {
+        const unsigned grid = (unsigned)((a.ngroups + kThreads - 1) / kThreads);
+        k_dense_reg<T, K><<<grid, kThreads, 0, s->stream>>>((c2_t<T> *)s->data, a, (const float4 *)d_mat,
+                                                            (const float2 *)d_mat);
+        e = cudaGetLastError();
+    }
+    pool_free(d_mat, s->stream);
+    // the host staging vectors are released on return: make the copy finish
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) PLK_FAIL(PLK_ERR_CUDA, std::string("dense matrix kernel: ") + cudaGetErrorString(e));
+    return PLK_OK;
+}
+
+template <class T>
+static int run_dense_reg(plk_state s, const std::vector<c2_t<T>> &hm, const WireGeom &g, int K) {
+    return K == 3 ? launch_dense_reg<T, 3>(s, hm, g) : launch_dense_reg<T, 4>(s, hm, g);
 }
 
 // Dense matrix application (any k <= kMaxDenseWires).  `matrix` is complex128
@@ -596,6 +745,7 @@ static int run_dense(plk_state s, const double *matrix, const int64_t *wires, in
         }
     WireGeom g;
     wire_geom(s->nq, wires, K, g);
+    if (K == 3 || K == 4) return run_dense_reg<T>(s, hm, g, K);
     std::vector<uint64_t> hoff(dim);
     for (int i = 0; i < dim; i++) hoff[i] = g.local_off(i);
     void *d_mat = nullptr, *d_off = nullptr;

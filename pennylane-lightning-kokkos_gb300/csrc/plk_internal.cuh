@@ -70,6 +70,19 @@ int device_ctx(int device, DeviceCtx **out);
 int pool_alloc(int device, void **ptr, size_t bytes, cudaStream_t stream);
 void pool_free(void *ptr, cudaStream_t stream);
 
+// Pool block released (stream-ordered) when the guard goes out of scope, on
+// every return path.
+struct PoolBuf {
+    void *p = nullptr;
+    cudaStream_t st = nullptr;
+    explicit PoolBuf(cudaStream_t s) : st(s) {}
+    PoolBuf(const PoolBuf &) = delete;
+    PoolBuf &operator=(const PoolBuf &) = delete;
+    ~PoolBuf() { pool_free(p, st); }
+    template <class U> U *as() const { return static_cast<U *>(p); }
+};
+
+
 constexpr int kThreads = 256;
 // Reductions use a fixed grid (a function of the device only) so that the
 // order of the FP64 partial sums, hence the result bits, never changes.
@@ -108,6 +121,27 @@ int check_wires(plk_state s, const int64_t *wires, int nw);
 // Make `s`'s stream wait for work queued so far on `other`'s stream.
 int order_after(plk_state s, plk_state other);
 int red_grid(const plk_state_s *s, uint64_t work_items);
+int device_sm_count(int device);
+// Grid of a reduction kernel: the blocks that fit on the device at once for
+// this kernel (a whole number per SM, so there is no partial last wave),
+// at most kMaxRedBlocks and no more than the work needs.  A function of the
+// kernel, the device and the size only, so the partial-sum order is fixed.
+template <class Kern>
+int red_grid_k(const plk_state_s *s, Kern kernel, uint64_t work_items, size_t dyn_smem = 0) {
+    const int sms = device_sm_count(s->device);
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, kThreads, dyn_smem) != cudaSuccess || occ < 1) {
+        cudaGetLastError();
+        occ = 1;
+    }
+    int per_sm = kMaxRedBlocks / (sms > 0 ? sms : 1);
+    if (per_sm > occ) per_sm = occ;
+    if (per_sm < 1) per_sm = 1;
+    uint64_t want = (work_items + kThreads - 1) / kThreads;
+    const uint64_t cap = (uint64_t)(sms > 0 ? sms : 1) * per_sm;
+    if (want > cap) want = cap;
+    return want < 1 ? 1 : (int)want;
+}
 // Grid for element-wise / grid-stride kernels on this state's device.
 int elem_grid(plk_state s, uint64_t work_items);
 // Set the state to basis vector |index> (InitView / setBasisStateFunctor).

@@ -112,6 +112,12 @@ bool c128_use_df() {
     return use;
 }
 
+int device_sm_count(int device) {
+    DeviceCtx *d = nullptr;
+    if (device_ctx(device, &d) != PLK_OK) return 1;
+    return d->sm_count;
+}
+
 int red_grid(const plk_state_s *s, uint64_t work_items) {
     DeviceCtx *d = nullptr;
     if (device_ctx(s->device, &d) != PLK_OK) return 1;

@@ -111,6 +111,23 @@ def test_dense_matrix_parity(k, dtype):
             np.testing.assert_allclose(s.get(), ref, atol=TOL[dtype] * scale, rtol=0)
 
 
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("k", [3, 4])
+def test_dense_matrix_large_state(k, dtype):
+    """3- and 4-wire matrices (one group per thread, amplitudes in registers)
+    on 16 qubits, with the wires at the highest, lowest and scattered bit
+    positions and in unsorted order."""
+    rng = np.random.default_rng(300 + k)
+    nq = 16
+    for wires in ([0, 1, 2, 3][:k], [15, 14, 13, 12][:k], [9, 0, 15, 4][:k], list(rng.choice(nq, k, False))):
+        m = haar(1 << k, rng)
+        psi = rand_state(nq, rng)
+        ref = O.apply_matrix(psi.copy(), m, [int(w) for w in wires], False)
+        s = State.from_array(psi, dtype)
+        s.apply_matrix(m, [int(w) for w in wires])
+        np.testing.assert_allclose(s.get(), ref, atol=TOL[dtype] * 4, rtol=0, err_msg=str(wires))
+
+
 def test_matrix_equals_named_gate():
     # Test_StateVectorKokkos_NonParam.cpp:932-1010, on random wires of 7 qubits
     rng = np.random.default_rng(2)

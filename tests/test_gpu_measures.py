@@ -68,6 +68,21 @@ def test_matrix_expval(k, dtype):
         assert abs(s.expval_matrix(m, wires) - ref) < ETOL[dtype] * 10 * (1 << k)
 
 
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_matrix_expval_general_matrix(k, dtype):
+    """Re<psi|M|psi> of a non-Hermitian matrix (the kernels evaluate the
+    Hermitian part) on 14 qubits, wires at both ends and scattered."""
+    rng = np.random.default_rng(40 + k)
+    nq = 14
+    psi = rand_state(nq, rng)
+    s = State.from_array(psi, dtype)
+    for wires in ([0, 1, 2][:k], [13, 12, 11][:k], [int(x) for x in rng.choice(nq, k, replace=False)]):
+        m = rng.normal(size=(1 << k, 1 << k)) + 1j * rng.normal(size=(1 << k, 1 << k))
+        ref = O.expval_matrix(psi, m, wires)
+        assert abs(s.expval_matrix(m, wires) - ref) < ETOL[dtype] * 10 * (1 << k), wires
+
+
 def test_expval_known_answers_gpu():
     s = State.from_array(KA.INI_3Q_C)
     assert s.expval_matrix(KA.HERMITIAN_3Q_MATRIX, [0, 1, 2]) == pytest.approx(KA.EXPVAL_HERMITIAN_3Q, rel=1e-7)
@@ -173,6 +188,44 @@ def test_probs_random_wires(dtype):
     for m in (1, 2, 3, 5, 8, 12, 13, 14):
         wires = [int(x) for x in rng.permutation(nq)[:m]]
         np.testing.assert_allclose(s.probs(wires), O.probs(psi, wires), atol=tol * 4, err_msg=str(wires))
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_probs_marginal_layouts(dtype):
+    """Marginals whose measured bits are the highest, the lowest, interleaved
+    or scattered, with many amplitudes per bin (chunked bins) and with fewer
+    than 32 amplitudes per bin (one thread per bin); repeated calls give the
+    same bits (fixed summation order)."""
+    rng = np.random.default_rng(16)
+    nq = 20
+    psi = rand_state(nq, rng)
+    s = State.from_array(psi, dtype)
+    tol = 1e-13 if dtype == N.PLK_C128 else 1e-6
+    ref_psi = s.get().astype(np.complex128)
+    cases = [[0], [nq - 1], [0, 1, 2], [nq - 3, nq - 2, nq - 1], [nq - 1, 0], list(range(0, nq, 2)),
+             list(range(13)), list(range(nq - 13, nq)), [int(x) for x in rng.permutation(nq)[:14]],
+             [int(x) for x in rng.permutation(nq)[:15]], [int(x) for x in rng.permutation(nq)[:17]],
+             [int(x) for x in rng.permutation(nq)]]
+    for wires in cases:
+        got = s.probs(wires)
+        np.testing.assert_allclose(got, O.probs(ref_psi, wires), atol=tol, rtol=0, err_msg=str(wires))
+        np.testing.assert_array_equal(got, s.probs(wires))
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("nq", [1, 5, 11, 12, 13, 20])
+def test_cdf_sizes(dtype, nq):
+    """Exclusive CDF for states smaller than one 4096-amplitude tile, exactly
+    one tile, a few tiles and many tiles."""
+    rng = np.random.default_rng(100 + nq)
+    psi = rand_state(nq, rng)
+    s = State.from_array(psi, dtype)
+    n = 1 << nq
+    cdf = np.empty(n)
+    N.check(N.lib.plk_cdf(s.h, cdf.ctypes.data_as(C.POINTER(C.c_double))))
+    ref = O.cdf_exclusive(O.probs(s.get().astype(np.complex128)))
+    np.testing.assert_allclose(cdf, ref, atol=1e-12, rtol=0)
+    assert cdf[0] == 0.0
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
