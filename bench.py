@@ -811,8 +811,8 @@ def run_kernels(args, device, torch):
                 a, m3.ctypes.data_as(C.POINTER(C.c_double)), P64(i64([hi, mid, lo])), 3, C.byref(v))), S),
             (f"expval 20 Pauli words ({npass_words} passes)", lambda: N.check(N.lib.plk_expval_pauli_sum(
                 a, len(co), PD(co), P64(of), P64(wi), le, C.byref(v))), npass_words * S),
-            ("apply 20 Pauli words (H|psi>)", lambda: N.check(N.lib.plk_apply_pauli_sum(
-                b, a, len(co), PD(co), P64(of), P64(wi), le)), 2 * S),
+            (f"apply 20 Pauli words (H|psi>, {npass_words} gathers)", lambda: N.check(N.lib.plk_apply_pauli_sum(
+                b, a, len(co), PD(co), P64(of), P64(wi), le)), (npass_words + 1) * S),
             ("inner product", lambda: N.check(N.lib.plk_inner_product(a, b, C.byref(vr), C.byref(vi))), 2 * S),
             ("axpy", lambda: N.check(N.lib.plk_state_axpy(b, 0.5, 0.25, a)), 3 * S),
             ("copy", lambda: N.check(N.lib.plk_state_copy(b, a)), 2 * S),

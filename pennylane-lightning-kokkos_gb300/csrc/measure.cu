@@ -155,12 +155,16 @@ __global__ void __launch_bounds__(kThreads)
     k_cdf_tile_sums(const c2_t<T> *__restrict__ sv, uint64_t n, double *__restrict__ tile_sum) {
     __shared__ double wsum[kThreads / 32];
     const uint64_t base = (uint64_t)blockIdx.x * kCdfTile;
-    DAcc acc;
-#pragma unroll 4
+    // all sixteen loads in flight before the sums
+    c2_t<T> v[kCdfPer];
+#pragma unroll
     for (int j = 0; j < kCdfPer; j++) {
         const uint64_t k = base + (uint64_t)j * kThreads + threadIdx.x;
-        if (k < n) acc.add(df_norm2(to_cdf(sv[k])));
+        v[j] = k < n ? sv[k] : mk<c2_t<T>>(0, 0);
     }
+    DAcc acc;
+#pragma unroll
+    for (int j = 0; j < kCdfPer; j++) acc.add(df_norm2(to_cdf(v[j])));
     double s = acc.value();
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -210,14 +214,20 @@ __global__ void __launch_bounds__(kThreads)
     __shared__ float2 wtot[kThreads / 32];
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const uint64_t base = (uint64_t)blockIdx.x * kCdfTile;
-    // 1. coalesced loads, |psi|^2 as double-float into shared memory
-#pragma unroll 4
-    for (int j = 0; j < kCdfPer; j++) {
-        const int e = j * kThreads + t;
-        const uint64_t k = base + e;
-        DF p = {0.0f, 0.0f};
-        if (k < n) p = df_norm2(to_cdf(sv[k]));
-        stage[cdf_slot(e)] = make_float2(p.hi, p.lo);
+    // 1. coalesced loads (all sixteen in flight), |psi|^2 as double-float
+    // into shared memory
+    {
+        c2_t<T> v[kCdfPer];
+#pragma unroll
+        for (int j = 0; j < kCdfPer; j++) {
+            const uint64_t k = base + (uint64_t)j * kThreads + t;
+            v[j] = k < n ? sv[k] : mk<c2_t<T>>(0, 0);
+        }
+#pragma unroll
+        for (int j = 0; j < kCdfPer; j++) {
+            const DF p = df_norm2(to_cdf(v[j]));
+            stage[cdf_slot(j * kThreads + t)] = make_float2(p.hi, p.lo);
+        }
     }
     __syncthreads();
     // 2. this thread's 16 consecutive values and their sum

@@ -194,6 +194,22 @@ def test_state_init_and_movers():
     np.testing.assert_array_equal(t.get(), e)
 
 
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("nq", [1, 9, 16])
+def test_axpy_real_and_complex(dtype, nq):
+    """y += a x (LinearAlgebraKokkos.hpp axpy_Kokkos) with a real and a
+    complex coefficient."""
+    rng = np.random.default_rng(70 + nq)
+    x, y = rand_state(nq, rng), rand_state(nq, rng)
+    tol = 1e-15 if dtype == N.PLK_C128 else 1e-6
+    for a in (0.75, -1.25 + 0.5j):
+        xs, ys = State.from_array(x, dtype), State.from_array(y, dtype)
+        N.check(N.lib.plk_state_axpy(ys.h, a.real, complex(a).imag, xs.h))
+        cast = (lambda v: v.astype(np.complex64).astype(np.complex128)) if dtype == N.PLK_C64 else (lambda v: v)
+        ref = cast(y) + a * cast(x)
+        np.testing.assert_allclose(ys.get(), ref, atol=tol * 4, rtol=0)
+
+
 def test_invalid_arguments_are_rejected():
     s = State(3)
     with pytest.raises(N.NativeError, match="out of range"):
