@@ -26,8 +26,8 @@ int plan_gate(int gate, int nw, bool inv, const double *prm, int np, GatePlan &p
 int plan_generator(int gate, int nw, GatePlan &p);
 int apply_gate_impl(plk_state s, int gate, const int64_t *wires, int nw, bool adj, const double *params, int np,
                     const double *matrix);
-int window_adjoint(plk_state lam, plk_state hl, const plk_op *ops, int nops, const int64_t *tp, int ntp, double *jac,
-                   bool &handled);
+int window_adjoint(plk_state lam, plk_state *hls, int nobs, const plk_op *ops, int nops, const int64_t *tp, int ntp,
+                   double *jac, bool &handled);
 
 static int adj_kind(int gate) {
     switch (gate) {
@@ -226,7 +226,7 @@ static int adjoint_run(plk_state work, plk_state *hlambda, int32_t nobs, const p
         st = plk_state_set_stream(hlambda[o], work->stream);
     }
     bool handled = false;
-    if (st == PLK_OK && nobs == 1) st = window_adjoint(work, hlambda[0], ops, nops, trainable, ntp, jac, handled);
+    if (st == PLK_OK) st = window_adjoint(work, hlambda, nobs, ops, nops, trainable, ntp, jac, handled);
     if (st == PLK_OK && !handled)
         st = work->dtype == PLK_C64 ? adjoint_impl<float>(work, hlambda, nobs, ops, nops, trainable, ntp, jac)
                                     : adjoint_impl<double>(work, hlambda, nobs, ops, nops, trainable, ntp, jac);

@@ -279,8 +279,8 @@ int window_apply_ops(plk_state s, const plk_op *ops, int nops, bool &handled) {
 
 // Backward sweep of the adjoint Jacobian with one observable (complex64);
 // `lam` is the working copy of the forward state (overwritten).
-int window_adjoint(plk_state lam, plk_state hl, const plk_op *ops, int nops, const int64_t *tp, int ntp, double *jac,
-                   bool &handled) {
+int window_adjoint(plk_state lam, plk_state *hls, int nobs, const plk_op *ops, int nops, const int64_t *tp, int ntp,
+                   double *jac, bool &handled) {
     handled = false;
     if (!window_path_enabled() || (lam->dtype != PLK_C64 && !c128_use_df()) || lam->nq < 6 || lam->nq > 32 ||
         ntp <= 0)
@@ -321,12 +321,39 @@ int window_adjoint(plk_state lam, plk_state hl, const plk_op *ops, int nops, con
     for (const auto &x : xs) seq.push_back(&x);
     PLK_TRY(wb.add_scheduled(seq));
     PLK_TRY(wb.close());
+    // Several observables: the program runs once per observable on a copy of
+    // lambda (the last one on lambda itself): 4 state passes per window per
+    // observable plus one copy, against 2 (1 + nobs) passes per op for the
+    // op-at-a-time kernel that carries every H lambda along.
+    if (nobs > 1 && (double)nobs * (4.0 * P.wins.size() + 2.0) > 2.0 * (1.0 + nobs) * xs.size()) return PLK_OK;
+    plk_state scratch = nullptr;
+    if (nobs > 1) {
+        if (plk_state_create(lam->nq, lam->dtype, lam->device, &scratch) != PLK_OK) {
+            // no room for a copy of lambda: the op-at-a-time path needs none
+            set_error(std::string());
+            return PLK_OK;
+        }
+    }
     handled = true;
+    int rc = PLK_OK;
+    if (scratch) rc = plk_state_set_stream(scratch, lam->stream);
     std::vector<double> j(ntp, 0.0);
-    if (lam->dtype == PLK_C64) PLK_TRY(run_program<float>(lam, hl, P, true, ntp, j.data()));
-    else PLK_TRY(run_program<double>(lam, hl, P, true, ntp, j.data()));
-    for (int t = 0; t < ntp; t++) jac[t] = j[t];
-    return PLK_OK;
+    for (int o = 0; o < nobs && rc == PLK_OK; o++) {
+        plk_state l = lam;
+        if (o + 1 < nobs) {
+            rc = plk_state_copy(scratch, lam);
+            l = scratch;
+        }
+        if (rc == PLK_OK)
+            rc = lam->dtype == PLK_C64 ? run_program<float>(l, hls[o], P, true, ntp, j.data())
+                                       : run_program<double>(l, hls[o], P, true, ntp, j.data());
+        if (rc == PLK_OK)
+            for (int t = 0; t < ntp; t++) jac[(size_t)o * ntp + t] = j[t];
+    }
+    const std::string err = rc == PLK_OK ? std::string() : last_error();
+    if (scratch) plk_state_destroy(scratch);
+    if (rc != PLK_OK) set_error(err);
+    return rc;
 }
 
 } // namespace plk

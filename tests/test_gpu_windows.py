@@ -175,3 +175,29 @@ def test_window_switch_roundtrip(window_switch):
     N.check(N.lib.plk_get_window_path(C.byref(v)))
     assert v.value == 1
 
+
+
+@pytest.mark.parametrize("dtype", [N.PLK_C64, N.PLK_C128])
+@pytest.mark.parametrize("nobs", [2, 5])
+def test_window_adjoint_several_observables(dtype, nobs, window_switch):
+    """Several observables: the window program runs once per observable on
+    a copy of lambda; rows match the oracle and the op-at-a-time path."""
+    rng = np.random.default_rng(200 + nobs)
+    nq = 10
+    ops = random_circuit(nq, 90, rng)
+    npar = sum(1 for o in ops if o[3])
+    trainable = sorted(int(x) for x in rng.choice(npar, max(1, npar * 3 // 4), replace=False))
+    obs = [("named", "PauliZ", [o % nq]) for o in range(nobs - 1)]
+    obs.append(("hamiltonian", [0.5, -1.2], [("named", "PauliX", [2]),
+                                             ("tensor", [("named", "PauliY", [0]), ("named", "PauliZ", [nq - 1])])]))
+    psi = O.run_ops(O.zero_state(nq), ops)
+    ref = O.adjoint_jacobian(psi, obs, ops, trainable)
+    window_switch(True)
+    jw = gpu_adjoint(psi, obs, ops, trainable, dtype)
+    jw2 = gpu_adjoint(psi, obs, ops, trainable, dtype)
+    window_switch(False)
+    jp = gpu_adjoint(psi, obs, ops, trainable, dtype)
+    np.testing.assert_array_equal(jw, jw2)
+    tol = 1e-10 if dtype == N.PLK_C128 else 1e-4
+    np.testing.assert_allclose(jw, ref, atol=tol, rtol=0)
+    np.testing.assert_allclose(jw, jp, atol=tol, rtol=0)
