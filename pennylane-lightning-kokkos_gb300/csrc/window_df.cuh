@@ -28,13 +28,19 @@ __device__ __forceinline__ DF df_norm(float h, float l) {
     return {s, __fsub_rn(l, __fsub_rn(s, h))};
 }
 
+// An op's outputs are formed afresh from error-free products: hi is the
+// rounded sum of the hi products and lo collects this op's rounding errors,
+// so |lo| stays within a few ulps of hi without renormalising, and the next
+// op's products (which take hi and lo as separate operands) lose nothing.
+// Ops therefore return their (hi, lo) pairs as they are.
+
 __device__ __forceinline__ CDF cdf_mul(const float4 e, const CDF &v) {
     float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
     df_first(e.x, e.y, v.re.hi, v.re.lo, rh, rl);
     df_mac(-e.z, -e.w, v.im.hi, v.im.lo, rh, rl);
     df_first(e.x, e.y, v.im.hi, v.im.lo, ih, il);
     df_mac(e.z, e.w, v.re.hi, v.re.lo, ih, il);
-    return {df_norm(rh, rl), df_norm(ih, il)};
+    return {{rh, rl}, {ih, il}};
 }
 
 // a * x + b * y for real double-floats a, b
@@ -42,7 +48,7 @@ __device__ __forceinline__ DF df_lin2(const DF &a, const DF &x, const DF &b, con
     float h, l;
     df_first(a.hi, a.lo, x.hi, x.lo, h, l);
     df_mac(b.hi, b.lo, y.hi, y.lo, h, l);
-    return df_norm(h, l);
+    return {h, l};
 }
 
 __device__ __forceinline__ DF df_neg(const DF &a) { return {-a.hi, -a.lo}; }
@@ -62,7 +68,7 @@ template <int K, int SEL> __device__ __forceinline__ void dense_apply_df(CDF (&v
             float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
 #pragma unroll
             for (int c = 0; c < D; c++) cdf_mac(U[r * D + c], in[c], rh, rl, ih, il);
-            v[j | spread<K, SEL>(r)] = {df_norm(rh, rl), df_norm(ih, il)};
+            v[j | spread<K, SEL>(r)] = {{rh, rl}, {ih, il}};
         }
     }
 }
@@ -205,7 +211,7 @@ static __device__ __noinline__ void dense_apply_df_rt(CDF *v, const float4 *__re
             int o = 0;
             for (int i = 0; i < K; i++)
                 if (r >> i & 1) o |= 1 << sb[i];
-            v[j | o] = {df_norm(rh, rl), df_norm(ih, il)};
+            v[j | o] = {{rh, rl}, {ih, il}};
         }
     }
 }
