@@ -778,6 +778,12 @@ def run_kernels(args, device, torch):
                                                           len(w), 0))
 
         sc, v, vr, vi = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        dptr, nq_, dt_ = C.c_void_p(), C.c_int(), C.c_int()
+        N.check(N.lib.plk_state_get(a, C.byref(nq_), C.byref(dt_), C.byref(dptr)))
+        dout = torch.zeros(16, dtype=torch.float64, device=f"cuda:{device}")
+        dout_p = C.cast(C.c_void_p(dout.data_ptr()), C.POINTER(C.c_double))
+        w16 = i64(list(range(15)) + [-1])
+        sp = C.c_void_p(stream.cuda_stream)
         zb = np.array([N.GATE_ID["PauliZ"]] * 20, dtype=np.int32)
         zw = i64(range(20))
         lo, mid, hi = nq - 3, nq // 2, 1  # wire -> rev bit: 2, ~n/2, n-2
@@ -805,6 +811,10 @@ def run_kernels(args, device, torch):
                                                                      C.byref(v))), S),
             ("expval 20 x PauliZ (one pass)", lambda: N.check(N.lib.plk_expval_named_batch(
                 a, 20, zb.ctypes.data_as(C.POINTER(C.c_int32)), P64(zw), PD(probs_m))), S),
+            ("expval PauliZ, allocation-free entry", lambda: N.check(N.lib.plk_expval_pauliz_noalloc(
+                dptr, nq, dtype, 1, P64(w16), dout_p, sp)), S),
+            ("expval 16 x PauliZ, allocation-free entry", lambda: N.check(N.lib.plk_expval_pauliz_noalloc(
+                dptr, nq, dtype, 16, P64(w16), dout_p, sp)), S),
             ("expval 2-qubit matrix", lambda: N.check(N.lib.plk_expval_matrix(
                 a, m2.ctypes.data_as(C.POINTER(C.c_double)), P64(i64([mid, lo])), 2, C.byref(v))), S),
             ("expval 3-qubit matrix", lambda: N.check(N.lib.plk_expval_matrix(

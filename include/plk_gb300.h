@@ -236,7 +236,7 @@ PLK_API int plk_adjoint_jacobian_inplace(plk_state lambda, plk_state *hlambda, i
  * of a caller-owned device state of 2^num_qubits amplitudes, written to the
  * caller-owned device array `out` (count doubles) on `cuda_stream`, with no
  * plk_state and no allocation.  Its scratch is a fixed library array
- * (32.25 KiB per GPU, held until the process exits) shared by every call:
+ * (128.25 KiB per GPU, held until the process exits) shared by every call:
  * count is limited to 16 (larger counts are rejected), and calls that overlap
  * on the GPU race.  Runs on the current device; the first call on a device
  * sets the scratch address up and should come before any stream capture. */

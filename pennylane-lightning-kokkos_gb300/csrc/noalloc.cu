@@ -10,9 +10,9 @@
 // and no allocation at all.
 //
 // Scratch: g_noalloc_scratch below, a file-scope __device__ array of
-// kNoAllocScratchBytes = 256 + 16 x 256 x 8 bytes (32.25 KiB): a 256-byte slot
-// for the blocks' ticket counter, then kNoAllocMaxValues x kNoAllocMaxBlocks
-// FP64 partial sums.  Every GPU that loads this library holds the array until
+// kNoAllocScratchBytes = 256 + 16 x 1024 x 8 bytes (128.25 KiB): a 256-byte
+// slot for the blocks' ticket counter, then kNoAllocMaxValues x
+// kNoAllocMaxBlocks FP64 partial sums.  Every GPU that loads this library holds the array until
 // the process exits.  All calls share it and it keeps the last call's
 // contents, so each call clears the counter first and rewrites every partial
 // it reads.  Calls that overlap on the GPU (different streams, or host threads
@@ -26,12 +26,12 @@
 #include <mutex>
 #include <string>
 
-#include "reduce.cuh"
+#include "expval_diag.cuh"
 
 namespace plk {
 
 constexpr int kNoAllocMaxValues = 16;
-constexpr int kNoAllocMaxBlocks = 256;
+constexpr int kNoAllocMaxBlocks = 1024;
 constexpr size_t kNoAllocCounterBytes = 256;
 constexpr size_t kNoAllocScratchBytes =
     kNoAllocCounterBytes + sizeof(double) * (size_t)kNoAllocMaxValues * kNoAllocMaxBlocks;
@@ -43,28 +43,41 @@ std::mutex g_noalloc_mutex;
 void *g_noalloc_ptr[64] = {nullptr};
 } // namespace
 
-struct ZMasks {
-    uint64_t z[kNoAllocMaxValues];
-};
-
-// One pass over the state: value v = sum_k |psi_k|^2 (-1)^popcount(k & z_v).
-template <class T>
-__global__ void __launch_bounds__(kThreads)
-    k_expval_diag_noalloc(const c2_t<T> *__restrict__ sv, uint64_t n, const ZMasks zm, int nv,
-                          unsigned char *__restrict__ scratch, double *__restrict__ out) {
-    double acc[kNoAllocMaxValues];
-#pragma unroll
-    for (int v = 0; v < kNoAllocMaxValues; v++) acc[v] = 0.0;
-    const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += step) {
-        const c2_t<T> a = sv[k];
-        const double p = (double)a.x * a.x + (double)a.y * a.y;
-#pragma unroll
-        for (int v = 0; v < kNoAllocMaxValues; v++) acc[v] += (__popcll(k & zm.z[v]) & 1) ? -p : p;
+// The same one-pass kernel as the regular entry points (expval_diag.cuh),
+// with its partial sums and ticket counter in the fixed scratch array and
+// the result written to the caller's buffer.  The grid is the kernel's
+// resident blocks per SM times the SM count (at most kNoAllocMaxBlocks),
+// found with the occupancy API, which allocates nothing.
+template <class T, int NV>
+static int launch_noalloc(const void *state, uint64_t n, const DiagMasks &zm, int nv, unsigned char *scr, double *out,
+                          cudaStream_t st, int sms) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_expval_diag<T, NV>, kThreads, 0) != cudaSuccess ||
+        occ < 1) {
+        cudaGetLastError();
+        occ = 1;
     }
-    auto *counter = reinterpret_cast<unsigned int *>(scratch);
-    auto *partials = reinterpret_cast<double *>(scratch + kNoAllocCounterBytes);
-    block_reduce_finish<kNoAllocMaxValues>(acc, partials, out, counter, 1.0, nv);
+    const uint64_t nquads = ((n + 127) >> 7) << 5;
+    uint64_t grid = (nquads + kThreads - 1) / kThreads;
+    const uint64_t cap = std::min<uint64_t>((uint64_t)kNoAllocMaxBlocks, (uint64_t)sms * (uint64_t)occ);
+    if (grid > cap) grid = cap;
+    if (grid < 1) grid = 1;
+    auto *counter = reinterpret_cast<unsigned int *>(scr);
+    auto *partials = reinterpret_cast<double *>(scr + kNoAllocCounterBytes);
+    k_expval_diag<T, NV><<<(unsigned)grid, kThreads, 0, st>>>((const c2_t<T> *)state, n, zm, nv, partials, out,
+                                                              counter);
+    PLK_CHECK_LAUNCH();
+    return PLK_OK;
+}
+
+template <class T>
+static int noalloc_dispatch(const void *state, uint64_t n, const DiagMasks &zm, int nv, unsigned char *scr,
+                            double *out, cudaStream_t st, int sms) {
+    if (nv == 1) return launch_noalloc<T, 1>(state, n, zm, nv, scr, out, st, sms);
+    if (nv == 2) return launch_noalloc<T, 2>(state, n, zm, nv, scr, out, st, sms);
+    if (nv <= 4) return launch_noalloc<T, 4>(state, n, zm, nv, scr, out, st, sms);
+    if (nv <= 8) return launch_noalloc<T, 8>(state, n, zm, nv, scr, out, st, sms);
+    return launch_noalloc<T, 16>(state, n, zm, nv, scr, out, st, sms);
 }
 
 static int noalloc_scratch(int device, void **out) {
@@ -101,7 +114,7 @@ PLK_API int plk_expval_pauliz_noalloc(const void *state, int32_t num_qubits, int
                                           std::to_string(kNoAllocMaxValues) + " values per call");
     if (((uintptr_t)state) % amp_bytes(dtype) != 0 || ((uintptr_t)out) % sizeof(double) != 0)
         PLK_FAIL(PLK_ERR_INVALID_ARG, "misaligned state or output pointer");
-    ZMasks zm{};
+    DiagMasks zm{};
     for (int i = 0; i < count; i++) {
         if (wires[i] < -1 || wires[i] >= num_qubits)
             PLK_FAIL(PLK_ERR_INVALID_ARG, "wire " + std::to_string(wires[i]) + " out of range (-1 = Identity)");
@@ -115,20 +128,11 @@ PLK_API int plk_expval_pauliz_noalloc(const void *state, int32_t num_qubits, int
     int sms = 0;
     PLK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     const uint64_t n = 1ULL << num_qubits;
-    uint64_t grid = (n + kThreads - 1) / kThreads;
-    const uint64_t cap = std::min<uint64_t>((uint64_t)kNoAllocMaxBlocks, (uint64_t)sms * 2);
-    if (grid > cap) grid = cap;
-    if (grid < 1) grid = 1;
     cudaStream_t st = (cudaStream_t)cuda_stream;
     PLK_CUDA(cudaMemsetAsync(scratch, 0, kNoAllocCounterBytes, st)); // ticket counter starts at zero
     auto *scr = static_cast<unsigned char *>(scratch);
-    if (dtype == PLK_C64)
-        k_expval_diag_noalloc<float><<<(unsigned)grid, kThreads, 0, st>>>((const float2 *)state, n, zm, count, scr, out);
-    else
-        k_expval_diag_noalloc<double><<<(unsigned)grid, kThreads, 0, st>>>((const double2 *)state, n, zm, count, scr,
-                                                                            out);
-    PLK_CHECK_LAUNCH();
-    return PLK_OK;
+    return dtype == PLK_C64 ? noalloc_dispatch<float>(state, n, zm, count, scr, out, st, sms)
+                            : noalloc_dispatch<double>(state, n, zm, count, scr, out, st, sms);
 }
 
 } // extern "C"
