@@ -33,16 +33,17 @@ __device__ __forceinline__ void diag_load_quad(const c2_t<T> *__restrict__ sv, u
     }
 }
 
-// up to 16 Z masks, passed by value (no allocation or copy per call)
+// up to 16 Z masks, passed by value (no allocation or copy per call); the
+// kernel reads them in place (__grid_constant__), with runtime indices
 struct DiagMasks {
     uint64_t z[16];
 };
 
 template <class T, int NV>
 __global__ void __launch_bounds__(kThreads)
-    k_expval_diag(const c2_t<T> *__restrict__ sv, uint64_t n, const DiagMasks zmask, int nv, double *partials,
-                  double *result, unsigned *counter) {
-    constexpr int U = sizeof(T) == 8 ? 1 : 2; // quads per batch
+    k_expval_diag(const c2_t<T> *__restrict__ sv, uint64_t n, const __grid_constant__ DiagMasks zmask, int nv,
+                  double *partials, double *result, unsigned *counter) {
+    constexpr int U = (sizeof(T) == 8 || NV >= 8) ? 1 : 2; // quads per batch (registers)
     __shared__ uint64_t zm[NV];
     __shared__ int zs[NV];
     for (int v = threadIdx.x; v < NV; v += blockDim.x) {
