@@ -345,19 +345,30 @@ __device__ void h_pass(const EngArgs<T> &a, const ECirc &ci, c2_t<T> *lam, c2_t<
     constexpr int NW = NT / 32;
     const uint32_t N = 1u << ci.nq;
     EAcc<T> acc;
+    constexpr int F = 4; // gathers issued together
     for (uint32_t i = t0; i < N; i += tstep) {
         const V li = eld<T, MODE>(lam, i);
         V hs = mk<V>(0, 0);
-        for (int k = 0; k < ci.nterms; k++) {
-            const ETerm tm = a.terms[ci.term0 + k];
-            const uint32_t j = i ^ tm.x;
-            const V v = eld<T, MODE>(lam, j);
-            const int q = (tm.ny + 2 * (__popc(j & tm.z) & 1)) & 3;
-            const V u = q == 0 ? v : (q == 1 ? mul_i(v) : (q == 2 ? cneg(v) : mul_mi(v)));
-            const T c = (T)tm.c;
-            hs = mk<V>(hs.x + c * u.x, hs.y + c * u.y);
-            if constexpr (sizeof(T) == 4) acc.re_dot_scaled(tm.ch, tm.cl, li, u);
-            else acc.re_dot_c(tm.c, li, u);
+        for (int k0 = 0; k0 < ci.nterms; k0 += F) {
+            // only the X masks are needed to issue the gathers; the rest of
+            // each term is read (from L1) when it is used
+            V v[F];
+#pragma unroll
+            for (int u = 0; u < F; u++)
+                if (k0 + u < ci.nterms) v[u] = eld<T, MODE>(lam, i ^ a.terms[ci.term0 + k0 + u].x);
+#pragma unroll
+            for (int u = 0; u < F; u++) {
+                if (k0 + u >= ci.nterms) break;
+                const ETerm tm = a.terms[ci.term0 + k0 + u];
+                const uint32_t j = i ^ tm.x;
+                const int q = (tm.ny + 2 * (__popc(j & tm.z) & 1)) & 3;
+                const V w = v[u];
+                const V x = q == 0 ? w : (q == 1 ? mul_i(w) : (q == 2 ? cneg(w) : mul_mi(w)));
+                const T c = (T)tm.c;
+                hs = mk<V>(hs.x + c * x.x, hs.y + c * x.y);
+                if constexpr (sizeof(T) == 4) acc.re_dot_scaled(tm.ch, tm.cl, li, x);
+                else acc.re_dot_c(tm.c, li, x);
+            }
         }
         est<T, MODE>(hl, i, hs);
     }
