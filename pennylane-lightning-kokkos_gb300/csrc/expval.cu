@@ -2,7 +2,8 @@
 //
 // Replaces ExpValFunctors.hpp, MeasuresKokkos::getExpectationValue*
 // (simulator/MeasuresKokkos.hpp:80-346) and the reductions / SpMV of
-// util/LinearAlgebraKokkos.hpp.  All reductions accumulate in FP64 (the
+// util/LinearAlgebraKokkos.hpp.  All reductions accumulate with FP64-class
+// precision (double-float on the FP32 pipe, FP64 across blocks; the
 // reference accumulates in the state precision) and are deterministic.
 #include <algorithm>
 #include <cstring>

@@ -11,9 +11,12 @@
 //             generators, the other amplitudes of the group), vectorised
 //             float2/double2 loads;
 //   k_quad  — the four amplitudes of a two-wire group;
-//   k_mrz   — element-wise parity phase (MultiRZ and its generator);
-//   k_dense — 2^k x 2^k matrices for k >= 3, group vectors staged in shared
-//             memory, matrix in shared memory when it fits.
+//   k_mrz   — element-wise parity phase (MultiRZ and its generator;
+//             k_mrz_df for complex128 in double-float);
+//   k_dense_reg — 2^k x 2^k matrices for k = 3, 4: one group per thread in
+//             registers, matrix in shared memory;
+//   k_dense — k >= 5, group vectors staged in shared memory, matrix in
+//             shared memory when it fits.
 #include <algorithm>
 #include <cmath>
 #include <cstring>

@@ -76,17 +76,19 @@ __global__ void __launch_bounds__(kThreads)
         const uint64_t o = it % nbins, c = it / nbins;
         const uint64_t base = marg_bin_offset(a, o) | marg_deposit(a, c << a.chunk_bits, a.chunk_bits) | lane_off;
         DAcc acc;
+        // cur walks the subsets of mid_mask in increasing order (masked
+        // increment: set the bits outside the mask, add one, clear them
+        // again); it is back at zero after the last subset
         uint64_t cur = 0;
         do {
-            // four loads in flight per lane
+            // up to four loads in flight per lane
             uint64_t ad[4];
             int cnt = 0;
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 ad[u] = base | cur;
-                if (cur != 0 || u == 0) cnt = u + 1;
-                cur = (cur | ~a.mid_mask) + 1;
-                cur &= a.mid_mask;
+                cnt = u + 1;
+                cur = ((cur | ~a.mid_mask) + 1) & a.mid_mask;
                 if (cur == 0) break;
             }
             c2_t<T> v[4];
