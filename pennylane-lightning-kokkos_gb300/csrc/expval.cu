@@ -407,17 +407,26 @@ __global__ void __launch_bounds__(kThreads)
             nb[u] = (x != 0 && g < items) ? sv[m ^ x] : zero;
         }
         if (single) {
-            // items past the end hold zero amplitudes: they add nothing
+            // items past the end hold zero amplitudes: they add nothing.
+            // px is uniform: one branch around the batch, so only the needed
+            // product is formed (complex128: two FP64 instructions per pair)
             float t = 0.0f;
+            V pa[U], pb[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                // Im(conj(a) b) = Re(conj(a) (-i b)): rotate b once when px
+                pa[u] = a[u];
+                pb[u] = px ? mk<V>(b[u].y, -b[u].x) : b[u];
+            }
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const uint64_t m = first_of(g0 + u * step);
                 const bool neg = __popcll(m & z1) & 1;
                 if constexpr (sizeof(T) == 4) {
-                    const float v = px ? fmaf(a[u].x, b[u].y, -a[u].y * b[u].x) : fmaf(a[u].x, b[u].x, a[u].y * b[u].y);
+                    const float v = fmaf(pa[u].x, pb[u].x, pa[u].y * pb[u].y);
                     t = fmaf(neg ? -cf : cf, v, t);
                 } else {
-                    const double v = px ? fma(a[u].x, b[u].y, -a[u].y * b[u].x) : fma(a[u].x, b[u].x, a[u].y * b[u].y);
+                    const double v = fma(pa[u].x, pb[u].x, pa[u].y * pb[u].y);
                     total.mac(neg ? DF{-cd.hi, -cd.lo} : cd, df_split(v));
                 }
             }
