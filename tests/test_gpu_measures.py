@@ -136,6 +136,33 @@ def test_pauli_sum_expval(dtype):
     assert abs(out.value - ref) < ETOL[dtype] * 20
 
 
+SINGLE_WORDS = [(0.9, [0], "X"), (-0.4, [12], "Y"), (1.3, [5], "Z"), (0.6, [0, 12], "XY"), (-1.1, [12, 0], "YY"),
+                (0.8, [3, 7], "XZ"), (0.5, [7, 3], "ZY"), (-0.7, [1, 6, 11], "YXZ"), (0.3, [2, 9, 4, 10], "YYYX"),
+                (1.2, [11, 10], "ZZ")]
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+def test_pauli_words_one_at_a_time(dtype):
+    """Each word on its own (one-term X groups: real and imaginary parts,
+    the pair's top bit low and high, diagonal words), on 13 qubits so that
+    the application kernel spans several 2048-amplitude tiles."""
+    rng = np.random.default_rng(31)
+    nq = 13
+    psi = rand_state(nq, rng)
+    s = State.from_array(psi, dtype)
+    ptol = 1e-12 if dtype == N.PLK_C128 else 2e-5
+    for word in SINGLE_WORDS:
+        ref = O.expval_observable(psi, pauli_obs([word]))
+        keep, (cp, op, wp, letters) = pauli_args([word])
+        out = C.c_double()
+        N.check(N.lib.plk_expval_pauli_sum(s.h, 1, cp, op, wp, letters, C.byref(out)))
+        assert abs(out.value - ref) < ETOL[dtype] * 4, word
+        hout = State(nq, dtype)
+        N.check(N.lib.plk_apply_pauli_sum(hout.h, s.h, 1, cp, op, wp, letters))
+        np.testing.assert_allclose(hout.get(), O.apply_observable(psi.copy(), pauli_obs([word])), atol=ptol * 4,
+                                   err_msg=str(word))
+
+
 @pytest.mark.parametrize("dtype", DTYPES)
 def test_apply_pauli_sum(dtype):
     rng = np.random.default_rng(4)
