@@ -58,6 +58,12 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import numpy as np  # noqa: E402
 
 METRIC = "gate HBM GB/s vs peak; adjoint grad s/circuit c64+FP64-acc vs c128 at stated err"
+# what bounds a gate kernel below the HBM roofline (from its ncu profile)
+KERNEL_LIMITS = {
+    "Haar2q": "FP32-pipe issue: the complex128 4x4 matrix runs in double-float, 16 error-free multiply-adds "
+              "per amplitude (about 275 FP32 instructions); DRAM traffic equals the algorithmic bytes; the "
+              "complex64 kernel runs at the copy rate",
+}
 GIB = 1 << 30
 
 
@@ -916,6 +922,8 @@ def main(argv=None):
             "frac": per_gate[dom]["GBps"] / peak, "peak_kind": peak_kind,
             "traffic": None, "launches": n_apps_dom,
             "overall_frac": value / (peak * world)}
+    if dom in KERNEL_LIMITS:
+        roof["limit"] = KERNEL_LIMITS[dom]
     prof = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(prof):
         try:
