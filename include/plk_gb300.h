@@ -244,10 +244,11 @@ PLK_API int plk_expval_pauliz_noalloc(const void *state, int32_t num_qubits, int
                                       const int64_t *wires, double *out, void *cuda_stream);
 
 /* ---- register-window path ----------------------------------------------- */
-/* Op lists (plk_apply_ops) and one-observable adjoint Jacobians run as
- * register-window sweeps (about seven ops per state pass; complex128 in
- * double-float on the FP32 pipe) unless this is switched off; results agree
- * with the op-at-a-time path to rounding. */
+/* Op lists (plk_apply_ops) and adjoint Jacobians run as register-window
+ * sweeps (about seven ops per state pass; complex128 in double-float on the
+ * FP32 pipe; with several observables one backward sweep per observable on
+ * a copy of lambda, when that moves fewer bytes) unless this is switched
+ * off; results agree with the op-at-a-time path to rounding. */
 PLK_API int plk_set_window_path(int32_t enable);
 PLK_API int plk_get_window_path(int32_t *enabled);
 
