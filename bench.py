@@ -20,8 +20,16 @@ Printed JSON line:
   roofline   - the gate kernel with the largest time share, against the
                measured HBM copy bandwidth
   per_gate   - GB/s and time share of every gate type (and wire range)
+  per_gate_fp64 - the same step with complex128 kernels in native IEEE FP64
+               arithmetic (the default is double-float on the FP32 pipe;
+               `dtype` says which ran)
   cpu_baseline - the oracle (CPU restatement of the reference functors) on
-               the host cores, a bounded sample of the same sweep
+               the host cores, one application per gate type and wire range
+  parity     - the GPU path against the oracle at the benchmarked sizes: the
+               30-qubit state after the cpu_baseline applications, the
+               26-qubit adjoint gradients (2 layers; all 40 with --only parity,
+               which also runs 31- and 32-qubit circuits), the 20-qubit
+               Jacobian
   adjoint_26q - adjoint Jacobian of the 26-qubit ansatz (40 layers of RY, RZ
                + CNOT ladder, 100-term Pauli Hamiltonian) in complex64 with
                FP64 accumulation vs complex128, seconds per gradient and the
@@ -33,8 +41,8 @@ Printed JSON line:
   plain_20q  - 20-qubit complex128 circuit (600 parameters), 20 <PauliZ> and
                the 20 x 600 Jacobian through the reference-facing module,
                against the oracle on the host cores
-  precision  - (--precision) 32-qubit complex64 vs 31-qubit complex128 at
-               equal bytes, 200-word Hamiltonian, error against complex128
+  precision  - 32-qubit complex64 vs 31-qubit complex128 at equal bytes,
+               200-word Hamiltonian, error against complex128
 `--impl reference` times the oracle (the CPU restatement of the reference
 functors) on the host cores instead.  For --gpus N
 under torchrun every rank runs an independent replica (weak scaling).
@@ -74,7 +82,8 @@ def parse_args(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--nq", type=int, default=30)
-    ap.add_argument("--reps", type=int, default=4, help="applications per gate and wire range per step")
+    ap.add_argument("--reps", type=int, default=4,
+                    help="applications per gate and wire range per step (the reference arm times one per step)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
@@ -83,11 +92,16 @@ def parse_args(argv=None):
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--batch-circuits", type=int, default=4096)
     ap.add_argument("--no-plain20", action="store_true")
-    ap.add_argument("--only", choices=["adjoint", "batch", "plain20", "precision", "kernels"], default=None,
-                    help="run one secondary config alone and print its JSON (profiling and spot checks)")
+    ap.add_argument("--only", choices=["adjoint", "batch", "plain20", "precision", "kernels", "parity"],
+                    default=None, help="run one secondary config alone and print its JSON (profiling, spot checks, "
+                                       "and the full-size oracle parity run)")
     ap.add_argument("--no-tune", action="store_true", help="batch: fixed launch configuration instead of autotuning")
-    ap.add_argument("--precision", action="store_true",
-                    help="also run the equal-bytes precision config (32-qubit complex64 vs 31-qubit complex128)")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the equal-bytes precision config (32-qubit complex64 vs 31-qubit complex128)")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the native-FP64 pass of the gate sweep")
+    ap.add_argument("--parity-layers", type=int, default=None,
+                    help="layers of the 26-qubit adjoint parity check against the oracle (default: 2 in the main "
+                         "run, 40 with --only parity)")
     ap.add_argument("--census-nq", type=int, default=26, help="--only kernels: state size in qubits")
     ap.add_argument("--census-reps", type=int, default=3, help="--only kernels: timed calls per entry point")
     return ap.parse_args(argv)
@@ -265,12 +279,46 @@ def run_device_sweep(args, device, torch, dist_barrier):
         nbytes = sum(plan[i]["touched"] * amp for i in range_groups[key])
         rng_ms[f"{key[0]}/{key[1]}"] = {"ms_per_app": ms / len(range_groups[key]),
                                        "GBps": nbytes / (ms * 1e6)}
+    fp64 = None if args.no_fp64 else fp64_pass(runner, groups, plan, amp, stream, torch, device)
     runner.close()
     return {
         "plan": plan, "groups": groups, "total_ms": total_ms, "per_gate_ms": per_gate_ms,
         "bytes_per_gate": bytes_per_gate, "total_bytes": total_bytes, "clocks": clk, "per_range": rng_ms,
-        "launches": len(plan) * args.steps,
+        "launches": len(plan) * args.steps, "fp64": fp64,
     }
+
+
+def fp64_pass(runner, groups, plan, amp, stream, torch, device):
+    """The same step with the complex128 kernels in native IEEE FP64
+    arithmetic instead of double-float (one warm-up step, one timed step):
+    the comparison figure for the double-float default."""
+    N = runner.N
+    before = N.c128_arithmetic()
+    N.set_c128_arithmetic("fp64")
+    mk = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    try:
+        for _, idx in groups:
+            for i in idx:
+                runner.apply(i)
+        torch.cuda.synchronize(device)
+        ev = [mk() for _ in range(len(groups) + 1)]
+        for gi, (_, idx) in enumerate(groups):
+            ev[gi].record(stream)
+            for i in idx:
+                runner.apply(i)
+        ev[-1].record(stream)
+        torch.cuda.synchronize(device)
+    finally:
+        N.set_c128_arithmetic(before)
+    per_gate, tot_ms, tot_b = {}, 0.0, 0.0
+    for gi, (g, idx) in enumerate(groups):
+        ms = ev[gi].elapsed_time(ev[gi + 1])
+        nbytes = sum(plan[i]["touched"] * amp for i in idx)
+        per_gate[g] = {"GBps": nbytes / (ms * 1e6), "ms_per_app": ms / len(idx)}
+        tot_ms += ms
+        tot_b += nbytes
+    return {"value": tot_b / (tot_ms * 1e6), "unit": "GB/s", "per_gate": per_gate,
+            "arithmetic": "native IEEE FP64 (complex128), one timed step"}
 
 
 # -------------------------------------------------------------------- e2e --
@@ -307,91 +355,182 @@ def run_e2e(args, device, torch, plan, steps):
 
 
 # ------------------------------------------------------------- CPU legs --
-def oracle_sweep(nq, plan, threads):
+def oracle_apply_plan(sv, plan):
     import oracle as O
 
-    O.set_num_threads(threads)
-    n = 1 << nq
-    sv = np.full(n, 1.0 / np.sqrt(n), dtype=np.complex128)
-    amp = 2 * n * 16
-    t = time.perf_counter()
-    nbytes = 0.0
     for a in plan:
         if a["matrix"] is not None:
             O.apply_matrix(sv, a["matrix"], a["wires"])
         else:
             O.apply(sv, a["name"], a["wires"], False, a["params"])
-        nbytes += a["touched"] * amp
+    return sv
+
+
+def oracle_sweep(nq, plan, threads):
+    """The oracle on |+>^n through `plan`: (GB/s, seconds, final state)."""
+    import oracle as O
+
+    O.set_num_threads(threads)
+    n = 1 << nq
+    sv = np.full(n, 1.0 / np.sqrt(n), dtype=np.complex128)
+    t = time.perf_counter()
+    oracle_apply_plan(sv, plan)
     dt = time.perf_counter() - t
-    return nbytes / dt / 1e9, dt
+    nbytes = sum(a["touched"] * 2 * n * 16 for a in plan)
+    return nbytes / dt / 1e9, dt, sv
 
 
 def run_cpu_baseline(args):
+    """The oracle on the host cores, one application per gate type and wire
+    range (27); also returns its final state and plan for the parity check."""
     from pennylane_lightning_kokkos.circuits import gate_sweep_plan
 
     threads = os.cpu_count() or 1
     plan = gate_sweep_plan(args.nq, 1, seed=2)
-    gbs, dt = oracle_sweep(args.nq, plan, threads)
+    gbs, dt, sv = oracle_sweep(args.nq, plan, threads)
     return {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
             "sample": f"{len(plan)} applications (1 per gate x wire range) on the {args.nq}-qubit complex128 "
-                      f"state, OpenMP oracle, {dt:.1f} s"}
+                      f"state, OpenMP oracle, {dt:.1f} s"}, sv, plan
+
+
+def max_abs_diff_chunked(a, b, chunk=1 << 26):
+    """max |a - b| over two large host arrays, a chunk at a time"""
+    m = 0.0
+    for off in range(0, a.size, chunk):
+        x = a[off:off + chunk].astype(np.complex128, copy=False)
+        m = max(m, float(np.max(np.abs(x - b[off:off + chunk]))))
+    return m
+
+
+def gpu_state_after(nq, dtype, device, prepare, plan=None, ops=None):
+    """Device state: `prepare` (a list of gate ops through plk_apply_ops, or
+    'hadamard' for H on every wire), then `plan` (sweep applications, one
+    C-ABI call each) or `ops` (one plk_apply_ops call); returned on the host."""
+    from pennylane_lightning_kokkos import _native as N
+
+    h = C.c_void_p()
+    N.check(N.lib.plk_state_create(nq, dtype, device, C.byref(h)))
+    keep = []
+
+    def apply_ops(lst):
+        arr = (N.PlkOp * len(lst))()
+        for i, (name, w, inv, p) in enumerate(lst):
+            wa = np.array(w, dtype=np.int64)
+            pa = np.array(p or [0.0], dtype=np.float64)
+            keep.extend([wa, pa])
+            arr[i] = N.PlkOp(N.GATE_ID[name], len(w), int(inv), len(p), wa.ctypes.data_as(C.POINTER(C.c_int64)),
+                             pa.ctypes.data_as(C.POINTER(C.c_double)), None)
+        N.check(N.lib.plk_apply_ops(h, arr, len(lst)))
+
+    try:
+        if prepare == "hadamard":
+            w = np.zeros(1, dtype=np.int64)
+            for wire in range(nq):
+                w[0] = wire
+                N.check(N.lib.plk_apply_gate(h, N.GATE_ID["Hadamard"], w.ctypes.data_as(C.POINTER(C.c_int64)), 1, 0,
+                                             None, 0))
+        elif prepare:
+            apply_ops(prepare)
+        for a in plan or []:
+            wa = np.array(a["wires"], dtype=np.int64)
+            wp = wa.ctypes.data_as(C.POINTER(C.c_int64))
+            if a["matrix"] is not None:
+                m = np.ascontiguousarray(a["matrix"], dtype=np.complex128)
+                N.check(N.lib.plk_apply_matrix(h, m.ctypes.data_as(C.POINTER(C.c_double)), wp, len(wa), 0))
+            else:
+                p = np.array(a["params"] or [0.0], dtype=np.float64)
+                N.check(N.lib.plk_apply_gate(h, N.GATE_ID[a["name"]], wp, len(wa), 0,
+                                             p.ctypes.data_as(C.POINTER(C.c_double)), len(a["params"])))
+        if ops:
+            apply_ops(ops)
+        out = np.empty(1 << nq, dtype=np.complex128 if dtype == N.PLK_C128 else np.complex64)
+        N.check(N.lib.plk_state_d2h(h, out.ctypes.data_as(C.c_void_p), out.size))
+    finally:
+        N.lib.plk_state_destroy(h)
+    return out
+
+
+def sweep_parity(args, device, sv_ref, plan):
+    """The GPU path on the same applications as the oracle leg, from |+>^n:
+    max |psi_gpu - psi_oracle| over all 2^n amplitudes (bar: 1e-12)."""
+    from pennylane_lightning_kokkos import _native as N
+
+    t = time.perf_counter()
+    got = gpu_state_after(args.nq, N.PLK_C128, device, "hadamard", plan=plan)
+    d = max_abs_diff_chunked(got, sv_ref)
+    del got
+    return {"qubits": args.nq, "applications": len(plan), "max_abs_state_diff_vs_oracle": d, "tolerance": 1e-12,
+            "pass": d <= 1e-12, "arithmetic": N.c128_arithmetic(), "seconds": time.perf_counter() - t}
+
+
+def sweep_config(args):
+    """The `config` of both arms: the workload whose rate both measure (a step
+    of either arm applies every gate type on every wire range equally often;
+    the arms differ only in how many applications a step holds, `step_plan`)."""
+    return {"workload": f"gate sweep, {args.nq} qubits complex128 ({(1 << args.nq) * 16 / GIB:.0f} GiB state), "
+                        "9 gate types x low/mid/high wire ranges, equal counts, seed 2",
+            "l2": "state larger than L2 (129 MB): no flush needed"}
 
 
 def run_reference_arm(args, rank):
     """--impl reference: the oracle (plain-C restatement of the reference's
-    Kokkos functors, OpenMP on every host core) on the same sweep; each step
-    is one application per gate type, cycling through the wire ranges."""
-    from pennylane_lightning_kokkos.circuits import gate_sweep_plan, wire_ranges
+    Kokkos functors, OpenMP on every host core) on the sweep workload, one
+    application per gate type and wire range per step, from |+>^n."""
+    from pennylane_lightning_kokkos.circuits import gate_sweep_plan
 
     if rank != 0:
         return None
-    threads = os.cpu_count() or 1
-    ranges = list(wire_ranges(args.nq))
-    full = gate_sweep_plan(args.nq, max(1, args.steps + args.warmup), seed=2)
-    by_key = {}
-    for a in full:
-        by_key.setdefault((a["name"], a["range"]), []).append(a)
-    steps = []
-    for k in range(args.warmup + args.steps):
-        r = ranges[k % len(ranges)]
-        steps.append([by_key[(g, r)][k // len(ranges)] for g in dict.fromkeys(a["name"] for a in full)])
     import oracle as O
 
+    threads = os.cpu_count() or 1
     O.set_num_threads(threads)
+    plan = gate_sweep_plan(args.nq, 1, seed=2)  # one application per gate type and wire range
     n = 1 << args.nq
     sv = np.full(n, 1.0 / np.sqrt(n), dtype=np.complex128)
-    amp = 2 * n * 16
-    for s in steps[:args.warmup]:
-        for a in s:
-            if a["matrix"] is not None:
-                O.apply_matrix(sv, a["matrix"], a["wires"])
-            else:
-                O.apply(sv, a["name"], a["wires"], False, a["params"])
+    for _ in range(args.warmup):
+        oracle_apply_plan(sv, plan)
     t = time.perf_counter()
-    nbytes = 0.0
-    for s in steps[args.warmup:]:
-        for a in s:
-            if a["matrix"] is not None:
-                O.apply_matrix(sv, a["matrix"], a["wires"])
-            else:
-                O.apply(sv, a["name"], a["wires"], False, a["params"])
-            nbytes += a["touched"] * amp
+    for _ in range(args.steps):
+        oracle_apply_plan(sv, plan)
     dt = time.perf_counter() - t
+    nbytes = sum(a["touched"] * 2 * n * 16 for a in plan) * args.steps
     value = nbytes / dt / 1e9
     return {
         "metric": METRIC, "value": value, "unit": "GB/s", "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / max(1, args.steps),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)",
-        "data": "synthetic (seeded gate sweep, seed 2)",
-        "config": {"workload": f"gate sweep, {args.nq} qubits complex128, 9 gate types x low/mid/high wires",
-                   "step": "one application per gate type, wire range cycling low/mid/high"},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "complex128 (native FP64, CPU oracle)", "data": "synthetic (seeded gate sweep, seed 2)",
+        "config": sweep_config(args),
+        "step_plan": f"{len(plan)} applications: 1 per gate type and wire range, the same every step",
         "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} steps x 9 applications, OpenMP oracle"},
+                         "sample": f"{args.steps} steps x {len(plan)} applications (one per gate type and wire "
+                                   "range), OpenMP oracle"},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
 # ------------------------------------------------------------ adjoint 26q --
+def module_gradient_fn(m, bits, device, nq, ops, words):
+    """A callable that runs one adjoint gradient of <H> through the
+    reference-facing module (state, tape, Hamiltonian of Pauli words)."""
+    dt = np.float64 if bits == "128" else np.float32
+    cdt = np.complex128 if bits == "128" else np.complex64
+    L = lambda name: getattr(m, name + "_C" + bits)  # noqa: E731
+    ham = _words_obs(m, bits, words)
+    adj = L("AdjointJacobianKokkos")()
+    tape = adj.create_ops_list([o[0] for o in ops], [np.array(o[3], dtype=dt) for o in ops], [o[1] for o in ops],
+                               [o[2] for o in ops], [np.array([], dtype=cdt)] * len(ops))
+    names, wires, invs, prms = [o[0] for o in ops], [o[1] for o in ops], [o[2] for o in ops], [o[3] for o in ops]
+    npar = sum(1 for o in ops if o[3])
+
+    def gradient():
+        sv = L("LightningKokkos")(nq, m.InitializationSettings().set_device_id(device))
+        sv.apply(names, wires, invs, prms)
+        return np.asarray(adj.adjoint_jacobian(sv, [ham], tape, list(range(npar))), dtype=np.float64)[0]
+
+    return gradient
+
+
 def run_adjoint(args, device, torch):
     import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
     from pennylane_lightning_kokkos.circuits import hardware_efficient_ansatz, random_pauli_words
@@ -403,25 +542,7 @@ def run_adjoint(args, device, torch):
     out = {"qubits": nq, "layers": layers, "params": npar, "ops": len(ops), "hamiltonian_terms": len(words)}
     grads = {}
     for bits in ("128", "64"):
-        dt = np.float64 if bits == "128" else np.float32
-        cdt = np.complex128 if bits == "128" else np.complex64
-        L = lambda name: getattr(m, name + "_C" + bits)  # noqa: E731
-        letters = {"X": "PauliX", "Y": "PauliY", "Z": "PauliZ"}
-        terms = []
-        for c, w, l in words:
-            fac = [L("NamedObsKokkos")(letters[x], [wi]) for wi, x in zip(w, l)]
-            terms.append(fac[0] if len(fac) == 1 else L("TensorProdObsKokkos")(fac))
-        ham = L("HamiltonianKokkos")(np.array([c for c, _, _ in words], dtype=dt), terms)
-        adj = L("AdjointJacobianKokkos")()
-        tape = adj.create_ops_list([o[0] for o in ops], [np.array(o[3], dtype=dt) for o in ops], [o[1] for o in ops],
-                                   [o[2] for o in ops], [np.array([], dtype=cdt)] * len(ops))
-        names, wires, invs, prms = [o[0] for o in ops], [o[1] for o in ops], [o[2] for o in ops], [o[3] for o in ops]
-
-        def gradient():
-            sv = L("LightningKokkos")(nq, m.InitializationSettings().set_device_id(device))
-            sv.apply(names, wires, invs, prms)
-            return np.asarray(adj.adjoint_jacobian(sv, [ham], tape, list(range(npar))), dtype=np.float64)[0]
-
+        gradient = module_gradient_fn(m, bits, device, nq, ops, words)
         gradient()  # warm-up (allocator pools, module load)
         torch.cuda.synchronize(device)
         reps = 2
@@ -433,7 +554,89 @@ def run_adjoint(args, device, torch):
         grads[bits] = g
     out["c64_speedup_vs_c128"] = out["c128_s_per_gradient"] / out["c64_s_per_gradient"]
     out["max_abs_grad_diff_c64_vs_c128"] = float(np.max(np.abs(grads["64"] - grads["128"])))
-    out["error_reference"] = "complex128 GPU path (parity-checked against the FP64 oracle at <= 20 qubits)"
+    out["error_reference"] = ("complex128 GPU path; both precisions against the FP64 oracle: the parity key "
+                              "(2 layers here, all 40 layers with --only parity)")
+    return out
+
+
+def run_adjoint_parity(args, device, torch, layers):
+    """The 26-qubit ansatz (RY, RZ on every wire + CNOT ladder, seed 4) with
+    `layers` layers and the 100-term Hamiltonian: adjoint gradients through
+    the module in complex128 and complex64 against the oracle's adjoint
+    Jacobian (FP64, host cores).  Bars: complex128 1e-10, complex64 1e-5."""
+    import oracle as O
+    import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
+    from pennylane_lightning_kokkos.circuits import hardware_efficient_ansatz, random_pauli_words
+
+    nq = args.adjoint_nq
+    ops = hardware_efficient_ansatz(nq, layers, seed=4, rotations=("RY", "RZ"), entangler="ladder")
+    words = random_pauli_words(nq, 100, seed=4)
+    npar = sum(1 for o in ops if o[3])
+    grads = {bits: module_gradient_fn(m, bits, device, nq, ops, words)() for bits in ("128", "64")}
+    torch.cuda.synchronize(device)
+    threads = os.cpu_count() or 1
+    O.set_num_threads(threads)
+    letters = {"X": "PauliX", "Y": "PauliY", "Z": "PauliZ"}
+    obs = ("hamiltonian", [c for c, _, _ in words],
+           [("tensor", [("named", letters[x], [wi]) for wi, x in zip(w, l)]) for _, w, l in words])
+    t = time.perf_counter()
+    psi = O.run_ops(O.zero_state(nq), ops)
+    ref = O.adjoint_jacobian(psi, [obs], ops, list(range(npar)))[0]
+    del psi
+    cpu_s = time.perf_counter() - t
+    d128 = float(np.max(np.abs(grads["128"] - ref)))
+    d64 = float(np.max(np.abs(grads["64"] - ref)))
+    return {"qubits": nq, "layers": layers, "params": npar, "ops": len(ops), "hamiltonian_terms": len(words),
+            "c128_max_abs_grad_diff_vs_oracle": d128, "c64_max_abs_grad_diff_vs_oracle": d64,
+            "max_abs_grad_oracle": float(np.max(np.abs(ref))), "tolerance": {"c128": 1e-10, "c64": 1e-5},
+            "pass": d128 <= 1e-10 and d64 <= 1e-5, "oracle_seconds": cpu_s, "oracle_cores": threads}
+
+
+def run_large_index_parity(device, nq, dtype_name):
+    """A short circuit at 31 qubits complex128 or 32 qubits complex64 (amplitude
+    indices beyond 2^31; the register-window path at its 32-qubit limit):
+    RY with seeded angles on every wire, then 12 ops on the highest, lowest
+    and middle wires, through plk_apply_ops; the whole state against the
+    oracle (FP64).  Bars: complex128 1e-12, complex64 5e-6."""
+    import oracle as O
+    from pennylane_lightning_kokkos import _native as N
+
+    rng = np.random.default_rng(31)
+    prep = [("RY", [w], False, [float(rng.uniform(0, np.pi))]) for w in range(nq)]
+    a = lambda: [float(rng.uniform(0, 2 * np.pi))]  # noqa: E731
+    lo, mid, hi = nq - 1, nq // 2, 0  # wire 0 is the most significant bit
+    ops = [("RY", [hi], False, a()), ("CNOT", [hi, lo], False, []), ("RZ", [lo], False, a()),
+           ("IsingXX", [hi, lo], False, a()), ("CRY", [lo, hi], False, a()), ("RX", [mid], False, a()),
+           ("CNOT", [lo, 1], False, []), ("RZ", [hi], False, a()), ("SingleExcitation", [1, lo], False, a()),
+           ("Hadamard", [hi], False, []), ("CZ", [hi, mid], False, []), ("RY", [lo], False, a())]
+    dtype = N.PLK_C128 if dtype_name == "c128" else N.PLK_C64
+    t = time.perf_counter()
+    got = gpu_state_after(nq, dtype, device, prep, ops=ops)
+    gpu_s = time.perf_counter() - t
+    O.set_num_threads(os.cpu_count() or 1)
+    t = time.perf_counter()
+    ref = O.run_ops(O.zero_state(nq), prep + ops)
+    cpu_s = time.perf_counter() - t
+    d = max_abs_diff_chunked(got, ref)
+    del got, ref
+    tol = 1e-12 if dtype_name == "c128" else 5e-6
+    return {"qubits": nq, "dtype": dtype_name, "ops": len(prep) + len(ops), "max_abs_state_diff_vs_oracle": d,
+            "tolerance": tol, "pass": d <= tol, "gpu_seconds_with_d2h": gpu_s, "oracle_seconds": cpu_s}
+
+
+def run_parity(args, device, torch):
+    """--only parity: every oracle comparison at the benchmarked sizes (30-qubit
+    sweep state, 26-qubit 40-layer adjoint gradients in both precisions,
+    31-qubit complex128 and 32-qubit complex64 short circuits)."""
+    layers = args.parity_layers or 40
+    out = {}
+    _, sv, plan = run_cpu_baseline(args)
+    out["sweep_state"] = sweep_parity(args, device, sv, plan)
+    del sv
+    out["large_index_c128_31q"] = run_large_index_parity(device, 31, "c128")
+    out["large_index_c64_32q"] = run_large_index_parity(device, 32, "c64")
+    out["adjoint_26q"] = run_adjoint_parity(args, device, torch, layers)
+    out["pass"] = all(v.get("pass", False) for v in out.values() if isinstance(v, dict))
     return out
 
 
@@ -890,7 +1093,7 @@ def main(argv=None):
     if args.only:
         if rank == 0:
             fn = {"adjoint": run_adjoint, "batch": run_batch, "plain20": run_plain20, "precision": run_precision,
-                  "kernels": run_kernels}
+                  "kernels": run_kernels, "parity": run_parity}
             print(json.dumps({args.only: fn[args.only](args, device, torch)}), flush=True)
         return 0
     dist = None
@@ -933,18 +1136,23 @@ def main(argv=None):
         except Exception:
             pass
 
+    from pennylane_lightning_kokkos import _native as N
+
+    dtype = ("complex128 storage, double-float arithmetic (FP32 pipe)" if N.c128_arithmetic() == "double-float"
+             else "complex128 (native FP64 arithmetic)")
     result = {
         "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic (seeded gate sweep, seed 2)",
-        "config": {"workload": f"gate sweep, {args.nq} qubits complex128 ({(1 << args.nq) * 16 / GIB:.0f} GiB state), "
-                               "9 gate types x low/mid/high wire ranges",
-                   "applications_per_step": len(sweep["plan"]), "reps_per_gate_and_range": args.reps,
-                   "l2": "state larger than L2 (129 MB): no flush needed",
-                   "parallelism": f"replicas x{world}"},
+        "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded gate sweep, seed 2)",
+        "config": sweep_config(args),
+        "step_plan": f"{len(sweep['plan'])} applications: {args.reps} per gate type and wire range, the same every "
+                     "step",
+        "parallelism": f"replicas x{world}",
         "roofline": roof, "per_gate": per_gate, "per_range": sweep["per_range"], "clocks": sweep["clocks"],
         "gpu_launches": sweep["launches"],
     }
+    if sweep["fp64"]:
+        result["per_gate_fp64"] = sweep["fp64"]
     if rank == 0 and not args.no_e2e:
         result["e2e"] = run_e2e(args, device, torch, sweep["plan"], steps=max(1, min(args.steps, 3)))
     if rank == 0 and not args.no_adjoint:
@@ -962,13 +1170,30 @@ def main(argv=None):
             result["plain_20q"] = run_plain20(args, device, torch)
         except Exception as e:
             result["plain_20q"] = {"error": repr(e)}
-    if rank == 0 and args.precision:
+    if rank == 0 and not args.no_precision:
         try:
             result["precision"] = run_precision(args, device, torch)
         except Exception as e:
             result["precision"] = {"error": repr(e)}
     if rank == 0 and not args.no_cpu:
-        result["cpu_baseline"] = run_cpu_baseline(args)
+        result["cpu_baseline"], sv_ref, plan_ref = run_cpu_baseline(args)
+        parity = {}
+        try:
+            parity["sweep_state"] = sweep_parity(args, device, sv_ref, plan_ref)
+        except Exception as e:
+            parity["sweep_state"] = {"error": repr(e)}
+        del sv_ref
+        if not args.no_adjoint:
+            try:
+                parity["adjoint_26q"] = run_adjoint_parity(args, device, torch, args.parity_layers or 2)
+            except Exception as e:
+                parity["adjoint_26q"] = {"error": repr(e)}
+        if "error" not in result.get("plain_20q", {"error": 1}):
+            p20 = result["plain_20q"]
+            parity["plain_20q"] = {k: p20[k] for k in ("max_abs_expval_diff_vs_oracle", "max_abs_jac_diff_vs_oracle")}
+        parity["full_size"] = ("bench.py --only parity: 26-qubit 40-layer gradients, 31/32-qubit short circuits; "
+                               "record in profiles/parity_full_size.md")
+        result["parity"] = parity
         if not args.no_batch and "error" not in result.get("batch", {}):
             try:
                 result["batch"]["cpu_oracle"] = run_batch_cpu(args)

@@ -252,6 +252,21 @@ PLK_API int plk_expval_pauliz_noalloc(const void *state, int32_t num_qubits, int
 PLK_API int plk_set_window_path(int32_t enable);
 PLK_API int plk_get_window_path(int32_t *enabled);
 
+/* ---- complex128 arithmetic ----------------------------------------------- */
+/* How complex128 kernels compute (storage is complex128 either way; no
+ * counterpart in the reference, whose Kokkos functors use native double).
+ * PLK_ARITH_DOUBLE_FLOAT (default): each double is carried as an unevaluated
+ * sum of two floats on the FP32 pipe (error-free products and sums, about
+ * 2^-45 relative error per gate; values below about 2^-103 lose their low
+ * part and below 2^-126 become zero), because this GPU's FP64 pipe is about
+ * 1/64 of its FP32 rate.  PLK_ARITH_FP64: native IEEE double arithmetic (and
+ * no register-window sweeps), slower for dense matrices and rotations.  The
+ * environment variable PLK_C128_ARITH=fp64 selects the initial mode; the
+ * setting applies to calls made after it. */
+enum { PLK_ARITH_DOUBLE_FLOAT = 0, PLK_ARITH_FP64 = 1 };
+PLK_API int plk_set_c128_arithmetic(int32_t mode);
+PLK_API int plk_get_c128_arithmetic(int32_t *mode);
+
 /* ---- gate matrices ---------------------------------------------------- */
 /* Dense matrix (row-major complex128 pairs, 4^num_wires of them; wires[0] is
  * the most significant bit of the row index) of a named gate, built from the

@@ -46,7 +46,12 @@ enum EKind : uint8_t {
     EK_DENSE = 1, // dense 2^K x 2^K matrix on K register bits (canonical order)
     EK_CX = 2,    // CNOT inside the window: a register permutation
     EK_DIAG = 3,  // diagonal gate on K <= 4 wires anywhere in the state
-    EK_PARITY = 4 // MultiRZ: phase by parity of the state bits in a mask
+    EK_PARITY = 4, // MultiRZ: phase by parity of the state bits in a mask
+    EK_DIAGSET = 5 // several diagonal ops on register bits merged into one 16-entry phase table
+                   // (complex128 single-state windows only): mat = the table; K = number of
+                   // trainable one-wire members, member m in bits 8m.. of `bits` (register bit,
+                   // generator codes of bit value 0 and 1: 0, 1 = +1, 2 = -1) and its reduction
+                   // slot in bits 4m.. of `gen`
 };
 
 // forms of one-wire dense matrices

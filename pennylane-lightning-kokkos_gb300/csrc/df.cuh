@@ -12,10 +12,11 @@
 // Conversions avoid the FP64 pipe: a double is split into hi (its top 24
 // significant bits, truncated) and lo (the next 23 bits) with integer
 // operations and one exact FP32 subtraction; a hi/lo pair becomes a double by
-// assembling each float's double encoding with integer operations and one
-// FP64 add.  Values below about 2^-97 in magnitude lose their lo part, values
-// below 2^-126 become zero; non-finite values are not supported on this path
-// (the native-FP64 kernels handle them).
+// assembling each float's double encoding with integer operations (the low
+// part scaled by 2^24 first, exactly) and one FP64 add.  Values below about
+// 2^-103 in magnitude lose their lo part, values below 2^-126 become zero;
+// non-finite values are not supported on this path (the native-FP64 kernels
+// handle them).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -50,17 +51,25 @@ __device__ __forceinline__ DF df_split(double x) {
     return r;
 }
 
-// The double with the same value as float f (normal floats; zero/denormal -> 0)
-__device__ __forceinline__ double df_f2d(float f) {
+// The double with the value f * 2^-k of a normal float f (zero and denormal
+// floats give 0), assembled with integer operations: no FP64-pipe conversion.
+__device__ __forceinline__ double df_f2d(float f, unsigned k = 0) {
     const unsigned b = __float_as_uint(f);
     const unsigned ef = (b >> 23) & 0xffu;
     if (ef == 0) return 0.0;
     const unsigned m = b & 0x7fffffu;
-    const unsigned hw = (b & 0x80000000u) | ((ef + 896u) << 20) | (m >> 3);
+    const unsigned hw = (b & 0x80000000u) | ((ef + 896u - k) << 20) | (m >> 3);
     return __hiloint2double((int)hw, (int)(m << 29));
 }
 
-__device__ __forceinline__ double df_join(float hi, float lo) { return __dadd_rn(df_f2d(hi), df_f2d(lo)); }
+// hi + lo as a double.  The low part is scaled by 2^24 first (exact: it is
+// at most about an ulp of hi, so the product stays finite, and a denormal
+// low part becomes a normal float), then assembled with its exponent
+// lowered by 24: small amplitudes keep their relative accuracy without a
+// branch.
+__device__ __forceinline__ double df_join(float hi, float lo) {
+    return __dadd_rn(df_f2d(hi), df_f2d(__fmul_rn(lo, 16777216.0f), 24u));
+}
 
 // (sh, sl) += a * b with a = ah + al, b = bh + bl; the accumulator is kept
 // unnormalised (sl collects the rounding errors).

@@ -654,8 +654,36 @@ template <class T, int NV> static void launch_diag(plk_state s, const DiagMasks 
                                                           w.d_result, w.d_counter);
 }
 
-// Diagonal (Identity / PauliZ) observables, up to 16 per pass.
+// Single-wire PauliZ / Identity values, up to kMaxRedValues per pass, at a
+// per-amplitude cost independent of their number (k_expval_zbits).
+template <class T> static int expval_zbits_impl(plk_state s, const std::vector<uint64_t> &zmasks, double *out) {
+    constexpr int M = sizeof(T) == 4 ? 5 : 4; // steps per lane per chunk: 2^M
+    const int total = (int)zmasks.size();
+    auto &w = s->ws;
+    const uint64_t chunks = (s->length + ((uint64_t)32 << M) - 1) / ((uint64_t)32 << M);
+    // one warp per chunk: work items are the chunks' warps' threads
+    const int grid = red_grid_k(s, k_expval_zbits<T, M>, chunks * 32);
+    for (int start = 0; start < total; start += kMaxRedValues) {
+        const int nv = std::min(kMaxRedValues, total - start);
+        ZBits zb;
+        for (int v = 0; v < nv; v++) {
+            const uint64_t z = zmasks[start + v];
+            zb.b[v] = z ? (int8_t)__builtin_ctzll(z) : (int8_t)-1;
+        }
+        k_expval_zbits<T, M><<<grid, kThreads, 0, s->stream>>>((const c2_t<T> *)s->data, s->length, zb, nv,
+                                                               w.d_partials, w.d_result, w.d_counter);
+        PLK_CHECK_LAUNCH();
+        PLK_TRY(fetch_results(s, nv, out + start));
+    }
+    return PLK_OK;
+}
+
+// Diagonal (Identity / PauliZ) observables: single-wire masks through
+// k_expval_zbits; masks of several bits up to 16 per pass (k_expval_diag).
 template <class T> static int expval_diag_impl(plk_state s, const std::vector<uint64_t> &zmasks, double *out) {
+    bool single = true;
+    for (uint64_t z : zmasks) single = single && (z & (z - 1)) == 0;
+    if (single) return expval_zbits_impl<T>(s, zmasks, out);
     const int total = (int)zmasks.size();
     for (int start = 0; start < total; start += 16) {
         const int nv = std::min(16, total - start);

@@ -131,4 +131,173 @@ __global__ void __launch_bounds__(kThreads)
     block_reduce_finish<NV>(acc, partials, result, counter, 1.0, nv);
 }
 
+// ---------------------------------------------------------------------------
+// Many single-wire PauliZ (and Identity) values in one pass, at a per-amplitude
+// cost that does not grow with their number.
+//
+// <Z_b> = sum_k p_k (-1)^(bit b of k), p_k = |psi_k|^2.  A warp reads chunks of
+// 32 * 2^M consecutive amplitudes: lane = index bits 0-4, step it = bits
+// 5 .. 5+M-1, chunk number = the bits above.  Each lane sums its 2^M values
+// as a binary tree whose level-l partial sums of odd blocks give
+// S_l = sum over steps with bit l set, so the lane keeps, across chunks, its
+// total and M sums S_l (about two additions per amplitude in all).  Then
+//   lane bits (b < 5):      sum over lanes of (-1)^(bit b of lane) total;
+//   step bits (5 <= b < 5+M): total - 2 S_(b-5);
+//   chunk bits (b >= 5+M):  per chunk, the warp's chunk sum with the sign of
+//                           the chunk's bit b, accumulated by the lane that
+//                           owns the observable (lane v % 32);
+//   Identity:               like a chunk bit that is never set.
+// complex64 forms the tree in FP32 and accumulates chunk sums in
+// double-float; complex128 works in double-float throughout.  Results are
+// reduced in a fixed order (bitwise reproducible for a given grid).
+struct ZBits {
+    int8_t b[kMaxRedValues]; // state bit of value v, -1: Identity
+};
+
+template <class T> struct ZTree; // per-lane binary-tree sums of 2^M values
+
+template <> struct ZTree<float> {
+    __device__ __forceinline__ static DF p(float2 v) { return {fmaf(v.x, v.x, v.y * v.y), 0.0f}; }
+    __device__ __forceinline__ static DF add(DF a, DF b) { return {a.hi + b.hi, 0.0f}; }
+};
+template <> struct ZTree<double> {
+    __device__ __forceinline__ static DF p(double2 v) { return df_norm2(to_cdf(v)); }
+    __device__ __forceinline__ static DF add(DF a, DF b) {
+        df_add(b.hi, b.lo, a.hi, a.lo);
+        return a;
+    }
+};
+
+// Streaming loads issued in program order (asm volatile), so that a lane's
+// loads of a chunk are all in flight before its first value is used.
+__device__ __forceinline__ double2 ld_stream(const double2 *p) {
+    double2 r;
+    asm volatile("ld.global.nc.v2.f64 {%0, %1}, [%2];" : "=d"(r.x), "=d"(r.y) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ float2 ld_stream(const float2 *p) {
+    float2 r;
+    asm volatile("ld.global.nc.v2.f32 {%0, %1}, [%2];" : "=f"(r.x), "=f"(r.y) : "l"(p));
+    return r;
+}
+
+template <class T, int M>
+__global__ void __launch_bounds__(kThreads)
+    k_expval_zbits(const c2_t<T> *__restrict__ sv, uint64_t n, const __grid_constant__ ZBits zb, int nv,
+                   double *partials, double *result, unsigned *counter) {
+    constexpr int STEPS = 1 << M;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int WPB = kThreads / 32;
+    const uint64_t chunk_amps = (uint64_t)32 << M;
+    const uint64_t nchunks = (n + chunk_amps - 1) / chunk_amps;
+    const uint64_t wstep = (uint64_t)gridDim.x * WPB;
+    // observables owned by this lane (chunk-bit and Identity values)
+    const int b0 = lane < nv ? zb.b[lane] : -2, b1 = lane + 32 < nv ? zb.b[lane + 32] : -2;
+    const bool own0 = b0 == -1 || b0 >= 5 + M, own1 = b1 == -1 || b1 >= 5 + M;
+    DAcc tot, S[M], h0, h1;
+    const bool whole = n >= chunk_amps; // every chunk lies inside the state
+    for (uint64_t c = (uint64_t)blockIdx.x * WPB + warp; c < nchunks; c += wstep) {
+        const uint64_t base = c * chunk_amps + lane;
+        c2_t<T> v[STEPS];
+        if (whole) {
+            // all of the chunk's loads in flight before the first is used
+#pragma unroll
+            for (int i = 0; i < STEPS; i++) v[i] = ld_stream(sv + base + (uint64_t)i * 32);
+        } else {
+#pragma unroll
+            for (int i = 0; i < STEPS; i++) {
+                const uint64_t k = base + (uint64_t)i * 32;
+                v[i] = k < n ? sv[k] : mk<c2_t<T>>(0, 0);
+            }
+        }
+        // binary tree over the steps: pend[l] holds the open even block of level l
+        DF pend[M + 1];
+        DF Sc[M];
+#pragma unroll
+        for (int l = 0; l < M; l++) Sc[l] = {0.0f, 0.0f};
+#pragma unroll
+        for (int i = 0; i < STEPS; i++) {
+            DF x = ZTree<T>::p(v[i]);
+#pragma unroll
+            for (int l = 0; l <= M; l++) {
+                if (l == M || !((i >> l) & 1)) { // even block at level l (or the chunk total)
+                    pend[l] = x;
+                    break;
+                }
+                Sc[l] = ZTree<T>::add(Sc[l], x); // odd block: its sum counts toward S_l
+                x = ZTree<T>::add(pend[l], x);
+            }
+        }
+        const DF ct = pend[M]; // this lane's total over the chunk
+        tot.add(ct);
+#pragma unroll
+        for (int l = 0; l < M; l++) S[l].add(Sc[l]);
+        if (__any_sync(0xffffffffu, own0 || own1)) {
+            // the warp's chunk sum, on every lane, in a fixed order
+            float sh = ct.hi, sl = ct.lo;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, sh, o);
+                const float ol = __shfl_xor_sync(0xffffffffu, sl, o);
+                df_add(oh, ol, sh, sl);
+            }
+            const uint64_t cb = c * chunk_amps;
+            if (own0) {
+                const bool neg = b0 >= 0 && ((cb >> b0) & 1);
+                h0.add(neg ? DF{-sh, -sl} : DF{sh, sl});
+            }
+            if (own1) {
+                const bool neg = b1 >= 0 && ((cb >> b1) & 1);
+                h1.add(neg ? DF{-sh, -sl} : DF{sh, sl});
+            }
+        }
+    }
+    // per-warp values, then per-block partials, then the last block sums them
+    __shared__ double sh[kMaxRedValues][WPB];
+    __shared__ bool is_last;
+    const double t = tot.value();
+    double sv_l[M];
+#pragma unroll
+    for (int l = 0; l < M; l++) sv_l[l] = S[l].value();
+    const double hv0 = h0.value(), hv1 = h1.value();
+    for (int vi = 0; vi < nv; vi++) {
+        const int b = zb.b[vi];
+        double x;
+        if (b == -1 || b >= 5 + M) {
+            x = (vi < 32) ? (lane == vi ? hv0 : 0.0) : (lane == vi - 32 ? hv1 : 0.0);
+        } else if (b < 5) {
+            x = ((lane >> b) & 1) ? -t : t;
+        } else {
+            double s = sv_l[0];
+#pragma unroll
+            for (int l = 1; l < M; l++) s = (b - 5 == l) ? sv_l[l] : s;
+            x = t - 2.0 * s;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[vi][warp] = x;
+    }
+    __syncthreads();
+    const int nblocks = gridDim.x;
+    for (int vi = threadIdx.x; vi < nv; vi += blockDim.x) {
+        double s = 0.0;
+        for (int w = 0; w < WPB; w++) s += sh[vi][w];
+        partials[(size_t)vi * nblocks + blockIdx.x] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) is_last = (atomicAdd(counter, 1u) == (unsigned)(nblocks - 1));
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    for (int vi = warp; vi < nv; vi += WPB) {
+        double s = 0.0;
+        for (int b = lane; b < nblocks; b += 32) s += __ldcg(partials + (size_t)vi * nblocks + b);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) result[vi] = s;
+    }
+    if (threadIdx.x == 0) *counter = 0u;
+}
+
 } // namespace plk

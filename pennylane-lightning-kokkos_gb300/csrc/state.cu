@@ -4,6 +4,7 @@
 // (simulator/StateVectorKokkos.hpp:140-574, 1596-1636) and the Kokkos
 // runtime configuration queries (util/GetConfigInfo.hpp).
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -104,13 +105,15 @@ static void pinned_put(double *p) {
     g_pinned_free.push_back(p);
 }
 
-bool c128_use_df() {
-    static const bool use = [] {
-        const char *v = std::getenv("PLK_C128_ARITH");
-        return !(v && std::string(v) == "fp64");
-    }();
-    return use;
-}
+// complex128 arithmetic: 1 = double-float on the FP32 pipe (default), 0 =
+// native FP64.  The environment sets the initial mode; plk_set_c128_arithmetic
+// changes it for the calls that follow (each launch reads it once).
+static std::atomic<int> g_c128_df{[] {
+    const char *v = std::getenv("PLK_C128_ARITH");
+    return (v && std::string(v) == "fp64") ? 0 : 1;
+}()};
+
+bool c128_use_df() { return g_c128_df.load(std::memory_order_relaxed) != 0; }
 
 int device_sm_count(int device) {
     DeviceCtx *d = nullptr;
@@ -247,6 +250,19 @@ extern "C" {
 PLK_API const char *plk_last_error(void) { return plk::last_error().c_str(); }
 
 PLK_API int plk_version(void) { return 1000; }
+
+PLK_API int plk_set_c128_arithmetic(int32_t mode) {
+    if (mode != PLK_ARITH_DOUBLE_FLOAT && mode != PLK_ARITH_FP64)
+        PLK_FAIL(PLK_ERR_INVALID_ARG, "complex128 arithmetic mode must be 0 (double-float) or 1 (FP64)");
+    plk::g_c128_df.store(mode == PLK_ARITH_DOUBLE_FLOAT ? 1 : 0);
+    return PLK_OK;
+}
+
+PLK_API int plk_get_c128_arithmetic(int32_t *mode) {
+    if (!mode) PLK_FAIL(PLK_ERR_INVALID_ARG, "null mode");
+    *mode = plk::c128_use_df() ? PLK_ARITH_DOUBLE_FLOAT : PLK_ARITH_FP64;
+    return PLK_OK;
+}
 
 PLK_API int plk_device_count(int *count) {
     if (!count) PLK_FAIL(PLK_ERR_INVALID_ARG, "null count");

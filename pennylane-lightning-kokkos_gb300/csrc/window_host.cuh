@@ -219,6 +219,9 @@ struct WinBuilder {
     std::vector<double2> &gen;
     int64_t &n_mats;
     std::vector<double2> *hmats = nullptr; // when set: matrices from XOp::umat, written here (no EPrep)
+    // merge runs of diagonal ops on register bits into EK_DIAGSET ops (needs
+    // hmats; only the complex128 single-state kernels implement the kind)
+    bool fuse_diag = false;
 
     std::vector<const XOp *> cur;
     uint32_t wbits = 0; // state bits of the open window
@@ -303,6 +306,60 @@ struct WinBuilder {
         return PLK_OK;
     }
 
+    // ------------------------------------------------ diagonal-run fusion --
+    static bool is_diagonal(const XOp &o) { return o.kind == EK_DIAG || o.kind == EK_PARITY; }
+
+    uint32_t state_bits(const XOp &o) const {
+        uint32_t m = 0;
+        if (o.kind == EK_PARITY)
+            for (int wv : o.mrz_wires) m |= 1u << (nq - 1 - wv);
+        else
+            for (int j = 0; j < o.K; j++) m |= 1u << (nq - 1 - o.wires[j]);
+        return m;
+    }
+
+    // Diagonal ops commute with each other; any two ops on disjoint wires
+    // commute.  Moving a diagonal op past an op it commutes with leaves every
+    // adjoint inner product unchanged: both states get the same unit-modulus
+    // phases, which cancel in <H lambda | G lambda> for a diagonal G, and a
+    // disjoint op commutes with the other op's generator.
+    bool commute(const XOp &a, const XOp &b) const {
+        return (is_diagonal(a) && is_diagonal(b)) || (state_bits(a) & state_bits(b)) == 0;
+    }
+
+    // a diagonal op whose phases depend only on the window's register bits;
+    // trainable ones only as one-wire members (their generator is a sign per
+    // register-bit value)
+    bool mergeable(const XOp &o, uint32_t w) const {
+        if (!is_diagonal(o) || (state_bits(o) & ~w) != 0) return false;
+        return !(bwd && o.slot >= 0) || (o.kind == EK_DIAG && o.K == 1);
+    }
+
+    // moves each diagonal op toward dir (-1: earlier, +1: later) past ops it
+    // commutes with, until it meets another diagonal op or an op it does not
+    // commute with; returns the order and the number of ops merging removes
+    std::vector<const XOp *> bubble(int dir, uint32_t w, int &saved) const {
+        std::vector<const XOp *> v = cur;
+        const int n = (int)v.size();
+        for (int t = 0; t < n; t++) {
+            const int i = dir < 0 ? t : n - 1 - t;
+            if (!is_diagonal(*v[i])) continue;
+            int k = i;
+            while (k + dir >= 0 && k + dir < n && !is_diagonal(*v[k + dir]) && commute(*v[k + dir], *v[k])) {
+                std::swap(v[k + dir], v[k]);
+                k += dir;
+            }
+        }
+        saved = 0;
+        for (int i = 0; i < n;) {
+            int j = i, m = 0;
+            while (j < n && is_diagonal(*v[j])) m += mergeable(*v[j++], w) ? 1 : 0;
+            if (m >= 2) saved += m - 1;
+            i = j > i ? j : i + 1;
+        }
+        return v;
+    }
+
     int close() {
         if (cur.empty()) return PLK_OK;
         // pad with the highest unused state bits (low bits stay with the
@@ -321,12 +378,48 @@ struct WinBuilder {
         for (const XOp *op : cur)
             if (!((op->kind == EK_DENSE && op->K == 1) || op->kind == EK_CX || (op->kind == EK_DIAG && op->K == 1)))
                 win.flags = 0;
+        // runs of diagonal ops on register bits become one phase table each
+        std::vector<std::vector<const XOp *>> groups; // emitted units: one op, or a merged run
+        if (fuse_diag && hmats) {
+            int s_left = 0, s_right = 0;
+            std::vector<const XOp *> vl = bubble(-1, w, s_left), vr = bubble(+1, w, s_right);
+            const std::vector<const XOp *> &v = s_left >= s_right ? vl : vr;
+            for (size_t i = 0; i < v.size();) {
+                if (!is_diagonal(*v[i])) {
+                    groups.push_back({v[i++]});
+                    continue;
+                }
+                std::vector<const XOp *> merge, rest;
+                while (i < v.size() && is_diagonal(*v[i])) (mergeable(*v[i], w) ? merge : rest).push_back(v[i++]);
+                // at most four trainable members per merged op
+                std::vector<const XOp *> g;
+                int ntr = 0;
+                for (const XOp *o : merge) {
+                    const bool tr = bwd && o->slot >= 0;
+                    if (tr && ntr == 4) {
+                        groups.push_back(g);
+                        g.clear();
+                        ntr = 0;
+                    }
+                    g.push_back(o);
+                    ntr += tr ? 1 : 0;
+                }
+                if (!g.empty()) groups.push_back(g);
+                for (const XOp *o : rest) groups.push_back({o});
+            }
+        } else {
+            for (const XOp *op : cur) groups.push_back({op});
+        }
         win.op0 = (int)ops.size();
-        win.nops = (int)cur.size();
+        win.nops = (int)groups.size();
         win.tr0 = (int)train.size();
         win.ntrain = 0;
-        for (const XOp *op : cur) {
-            const XOp &o = *op;
+        for (const auto &grp : groups) {
+            if (grp.size() > 1) {
+                PLK_TRY(emit_diagset(grp, pos, win));
+                continue;
+            }
+            const XOp &o = *grp[0];
             EOp e;
             std::memset(&e, 0, sizeof(e));
             e.kind = (uint8_t)o.kind;
@@ -455,6 +548,59 @@ struct WinBuilder {
         cur.clear();
         wbits = 0;
         ntrain = 0;
+        return PLK_OK;
+    }
+
+    // One EK_DIAGSET op: the product of the group's diagonals as 16 phases
+    // over the register index, and its trainable one-wire members.
+    int emit_diagset(const std::vector<const XOp *> &grp, const int *pos, EWin &win) {
+        EOp e;
+        std::memset(&e, 0, sizeof(e));
+        e.kind = EK_DIAGSET;
+        e.red = 0xff;
+        e.mat = (int32_t)n_mats;
+        double2 ph[kWinAmps];
+        for (int j = 0; j < kWinAmps; j++) ph[j] = mk<double2>(1.0, 0.0);
+        int nm = 0;
+        for (const XOp *op : grp) {
+            const XOp &o = *op;
+            for (int j = 0; j < kWinAmps; j++) {
+                int li = 0, Dm = 2;
+                if (o.kind == EK_PARITY) {
+                    int par = 0;
+                    for (int wv : o.mrz_wires) par ^= (j >> pos[nq - 1 - wv]) & 1;
+                    li = par;
+                } else {
+                    Dm = 1 << o.K;
+                    for (int q = 0; q < o.K; q++) li |= ((j >> pos[nq - 1 - o.wires[q]]) & 1) << (o.K - 1 - q);
+                }
+                double2 z = o.umat[(size_t)li * Dm + li];
+                if (bwd) z.y = -z.y;
+                ph[j] = cmul(ph[j], z);
+            }
+            if (bwd && o.slot >= 0) {
+                GatePlan gp;
+                PLK_TRY(plan_generator(o.gate, 1, gp));
+                std::vector<double2> G;
+                plan_dense(gp, 1, G);
+                auto code = [](double2 z) -> uint32_t {
+                    if (z.y != 0.0 || (z.x != 0.0 && z.x != 1.0 && z.x != -1.0)) return 3u; // not a real sign
+                    return z.x == 0.0 ? 0u : (z.x > 0.0 ? 1u : 2u);
+                };
+                const uint32_t c0 = code(G[0]), c1 = code(G[3]);
+                if (c0 == 3u || c1 == 3u) PLK_FAIL(PLK_ERR_UNSUPPORTED, "internal: diagonal generator is not real");
+                const int rbit = pos[nq - 1 - o.wires[0]];
+                e.bits |= ((uint32_t)rbit | (c0 << 2) | (c1 << 4)) << (8 * nm);
+                e.gen |= (int32_t)win.ntrain << (4 * nm);
+                train.push_back(ETrain{o.slot, (float)(-2.0 * gp.scale * (o.inv ? -1.0 : 1.0))});
+                win.ntrain++;
+                nm++;
+            }
+        }
+        e.K = (uint8_t)nm;
+        for (int j = 0; j < kWinAmps; j++) hmats->push_back(ph[j]);
+        n_mats += kWinAmps;
+        ops.push_back(e);
         return PLK_OK;
     }
 };

@@ -69,11 +69,12 @@ __global__ void __launch_bounds__(kWinThreads, 2)
     }
 }
 
-// complex128 windows (windows_df.cu, windows_df_fwd.cu; the slim variant of
-// the complex64 kernels measured no faster there, double-float work dominates)
+// complex128 windows (windows_df.cu, windows_df_fwd.cu: shared-memory staged
+// double-float kernels, 128 threads per CTA)
+int window_df_grid(int sm_count, uint64_t groups, bool bwd);
 void launch_window_df_bwd(int grid, cudaStream_t st, double2 *lam, double2 *hl, int nq, const EWin *wins, int wi,
-                          const EOp *ops, const float4 *mats, const ETrain *train, double *bpart, int in_df,
-                          int out_df);
+                          int ntrain, const EOp *ops, const float4 *mats, const ETrain *train, double *bpart,
+                          int in_df, int out_df);
 void launch_window_df_fwd(int grid, cudaStream_t st, double2 *lam, double2 *hl, int nq, const EWin *wins, int wi,
                           const EOp *ops, const float4 *mats, const ETrain *train, double *bpart, int in_df,
                           int out_df);
@@ -149,6 +150,64 @@ static int make_xop(const plk_op &op, int nq, XOp &x, bool &fits) {
     return PLK_OK;
 }
 
+// Every index a window kernel will follow, checked on the host before the
+// first launch: matrix and generator offsets inside the matrix buffer,
+// register-bit selections, reduction slots below the window's trainable
+// count, Jacobian slots below ntp.  A failed check is an internal error
+// reported to the caller, never a launch.
+static int validate_program(const StateProgram &P, const std::vector<EOp> &ops, int nq, size_t nmats, bool bwd,
+                            int ntp) {
+    auto bad = [](const std::string &what) {
+        set_error("internal: window program check failed: " + what);
+        return PLK_ERR_UNSUPPORTED;
+    };
+    for (size_t wi = 0; wi < P.wins.size(); wi++) {
+        const EWin &w = P.wins[wi];
+        if (w.op0 < 0 || w.nops < 0 || (size_t)w.op0 + w.nops > ops.size()) return bad("window op range");
+        if (w.ntrain < 0 || w.ntrain > kMaxWinTrain || w.tr0 < 0 || (size_t)w.tr0 + w.ntrain > P.train.size())
+            return bad("window trainable range");
+        for (int i = 0; i < 4; i++)
+            if (w.rb[i] >= nq || (i > 0 && w.rb[i] <= w.rb[i - 1])) return bad("window register bits");
+        for (int t = 0; t < w.ntrain; t++)
+            if (P.train[w.tr0 + t].slot < 0 || P.train[w.tr0 + t].slot >= std::max(1, ntp))
+                return bad("Jacobian slot");
+        for (int k = 0; k < w.nops; k++) {
+            const EOp &o = ops[w.op0 + k];
+            const bool tr = bwd && o.red != 0xff;
+            if (o.red != 0xff && (!bwd || o.red >= w.ntrain)) return bad("reduction slot");
+            auto in_mats = [&](int64_t off, int64_t len) { return off >= 0 && off + len <= (int64_t)nmats; };
+            const int D = 1 << (o.K > 4 ? 4 : o.K);
+            switch (o.kind) {
+            case EK_DENSE:
+                if (o.K < 1 || o.K > 4 || !in_mats(o.mat, (int64_t)D * D)) return bad("dense op matrix");
+                if ((o.K == 1 && ((o.sel >> 2) > 2)) || (o.K == 2 && o.sel > 5) || (o.K == 3 && o.sel > 3))
+                    return bad("dense op bits");
+                if (tr && o.K > 1 && !in_mats(o.gen, (int64_t)D * D)) return bad("dense generator");
+                break;
+            case EK_CX:
+                if ((o.sel >> 2) > 3 || (o.sel >> 2) == (o.sel & 3)) return bad("CNOT bits");
+                break;
+            case EK_DIAG:
+                if (o.K < 1 || o.K > 4 || !in_mats(o.mat, D) || o.sel > 4) return bad("diagonal op");
+                for (int j = 0; j < o.K; j++)
+                    if (((o.bits >> (5 * j)) & 31u) >= (uint32_t)nq) return bad("diagonal op wire");
+                if (tr && !in_mats(o.gen, D)) return bad("diagonal generator");
+                break;
+            case EK_PARITY:
+                if (!in_mats(o.mat, 2) || (nq < 32 && (o.bits >> nq) != 0)) return bad("parity op");
+                break;
+            case EK_DIAGSET:
+                if (o.K > 4 || !in_mats(o.mat, kWinAmps) || (o.K > 0 && !bwd)) return bad("merged diagonal");
+                for (int m = 0; m < o.K; m++)
+                    if (((o.gen >> (4 * m)) & 15) >= w.ntrain) return bad("merged diagonal member");
+                break;
+            default: return bad("op kind");
+            }
+        }
+    }
+    return PLK_OK;
+}
+
 template <class T>
 static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool bwd, int ntp, double *jac_host) {
     using V = c2_t<T>;
@@ -156,9 +215,10 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
     PLK_TRY(device_ctx(lam->device, &d));
     cudaStream_t st = lam->stream;
     const uint64_t nu = lam->length >> kWinBits;
-    const int per_sm = std::is_same<T, double>::value ? 1 : 2; // register budget of the df kernels
-    const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)d->sm_count * per_sm,
-                                                                    (nu + kWinThreads - 1) / kWinThreads));
+    const int grid = std::is_same<T, double>::value
+                         ? window_df_grid(d->sm_count, nu, bwd)
+                         : (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)d->sm_count * 2,
+                                                                         (nu + kWinThreads - 1) / kWinThreads));
     // matrices: state precision for complex64, split double-floats for complex128
     using M = typename std::conditional<std::is_same<T, double>::value, float4, V>::type;
     std::vector<M> mats(P.mats.size() + P.gen.size());
@@ -175,8 +235,9 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
     for (size_t i = 0; i < P.mats.size(); i++) mats[i] = conv(P.mats[i]);
     for (size_t i = 0; i < P.gen.size(); i++) mats[P.mats.size() + i] = conv(P.gen[i]);
     std::vector<EOp> ops = P.ops;
-    for (auto &o : ops)
-        if (o.gen >= 0) o.gen += (int32_t)P.mats.size();
+    for (auto &o : ops) // generators follow the matrices (EK_DIAGSET keeps reduction slots in gen)
+        if (o.gen >= 0 && o.kind != EK_DIAGSET) o.gen += (int32_t)P.mats.size();
+    PLK_TRY(validate_program(P, ops, lam->nq, mats.size(), bwd, ntp));
     const size_t b_w = P.wins.size() * sizeof(EWin), b_o = ops.size() * sizeof(EOp);
     const size_t b_t = std::max<size_t>(1, P.train.size()) * sizeof(ETrain), b_m = std::max<size_t>(1, mats.size()) * sizeof(M);
     const size_t b_p = bwd ? (size_t)std::max(1, ntp) * grid * sizeof(double) : 0;
@@ -216,8 +277,11 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
         const bool slim = P.wins[wi].flags & 1;
         if constexpr (std::is_same<T, double>::value) {
             const int in_df = wi > 0, out_df = wi + 1 < P.wins.size();
-if (bwd) launch_window_df_bwd(grid, st, lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p, in_df, out_df);
-            else launch_window_df_fwd(grid, st, lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p, in_df, out_df);
+            if (bwd)
+                launch_window_df_bwd(grid, st, lp, hp, lam->nq, d_w, (int)wi, P.wins[wi].ntrain, d_o, d_m, d_t, d_p,
+                                     in_df, out_df);
+            else
+                launch_window_df_fwd(grid, st, lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p, in_df, out_df);
         } else {
 #define PLK_W(B_, S_) k_state_window<T, B_, S_><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p)
             if (bwd) {
@@ -268,6 +332,7 @@ int window_apply_ops(plk_state s, const plk_op *ops, int nops, bool &handled) {
     StateProgram P;
     WinBuilder wb{s->nq, false, P.wins, P.ops, P.train, P.prep, P.gen, P.n_mats};
     wb.hmats = &P.mats;
+    wb.fuse_diag = s->dtype == PLK_C128; // merged diagonal runs: complex128 kernels only
     std::vector<const XOp *> seq;
     for (const auto &x : xs) seq.push_back(&x);
     PLK_TRY(wb.add_scheduled(seq));
@@ -317,6 +382,7 @@ int window_adjoint(plk_state lam, plk_state *hls, int nobs, const plk_op *ops, i
     StateProgram P;
     WinBuilder wb{lam->nq, true, P.wins, P.ops, P.train, P.prep, P.gen, P.n_mats};
     wb.hmats = &P.mats;
+    wb.fuse_diag = lam->dtype == PLK_C128; // merged diagonal runs: complex128 kernels only
     std::vector<const XOp *> seq;
     for (const auto &x : xs) seq.push_back(&x);
     PLK_TRY(wb.add_scheduled(seq));

@@ -23,6 +23,7 @@ lib = C.CDLL(LIB_PATH)
 
 PLK_OK = 0
 PLK_C64, PLK_C128 = 0, 1
+PLK_ARITH_DOUBLE_FLOAT, PLK_ARITH_FP64 = 0, 1
 STATUS_NAMES = {0: "OK", 1: "INVALID_ARG", 2: "UNKNOWN_GATE", 3: "CUDA", 4: "OUT_OF_MEMORY", 5: "UNSUPPORTED",
                 6: "NO_DEVICE"}
 
@@ -101,6 +102,8 @@ _SIGS = {
     "plk_expval_pauliz_noalloc": ([_vp, C.c_int32, C.c_int32, C.c_int32, _i64p, _dp, _vp], C.c_int),
     "plk_set_window_path": ([C.c_int32], C.c_int),
     "plk_get_window_path": ([_i32p], C.c_int),
+    "plk_set_c128_arithmetic": ([C.c_int32], C.c_int),
+    "plk_get_c128_arithmetic": ([_i32p], C.c_int),
     "plk_gate_matrix": ([C.c_int32, _dp, C.c_int32, C.c_int32, C.c_int32, _dp], C.c_int),
     "plk_batch_create": ([C.c_int32, C.c_int32, C.POINTER(_vp)], C.c_int),
     "plk_batch_destroy": ([_vp], C.c_int),
@@ -150,6 +153,20 @@ def gate_matrix(name: str, params=(), num_wires: int | None = None, adjoint: boo
     out = np.zeros(2 * (1 << (2 * nw)), dtype=np.float64)
     check(lib.plk_gate_matrix(g, prm.ctypes.data_as(_dp), len(prm), int(adjoint), nw, out.ctypes.data_as(_dp)))
     return out.view(np.complex128).reshape(1 << nw, 1 << nw)
+
+
+def c128_arithmetic() -> str:
+    """'double-float' (FP32 pipe, the default) or 'fp64' (native IEEE double)."""
+    m = C.c_int32()
+    check(lib.plk_get_c128_arithmetic(C.byref(m)))
+    return "fp64" if m.value == PLK_ARITH_FP64 else "double-float"
+
+
+def set_c128_arithmetic(mode: str) -> None:
+    """Select how complex128 kernels compute: 'double-float' or 'fp64'."""
+    if mode not in ("double-float", "fp64"):
+        raise ValueError("mode must be 'double-float' or 'fp64'")
+    check(lib.plk_set_c128_arithmetic(PLK_ARITH_FP64 if mode == "fp64" else PLK_ARITH_DOUBLE_FLOAT))
 
 
 def device_info(device: int = 0) -> dict:

@@ -109,6 +109,23 @@ def test_observables_build_without_device():
     assert "RX" in repr(ops)
 
 
+def test_c128_arithmetic_switch():
+    # the mode is host state only: set, read back, reject unknown modes, restore
+    from pennylane_lightning_kokkos import _native as N
+
+    before = N.c128_arithmetic()
+    try:
+        N.set_c128_arithmetic("fp64")
+        assert N.c128_arithmetic() == "fp64"
+        N.set_c128_arithmetic("double-float")
+        assert N.c128_arithmetic() == "double-float"
+        assert N.lib.plk_set_c128_arithmetic(7) == 1  # PLK_ERR_INVALID_ARG
+        assert "arithmetic mode" in N.last_error()
+        assert N.c128_arithmetic() == "double-float"
+    finally:
+        N.set_c128_arithmetic(before)
+
+
 @pytest.mark.skipif(os.environ.get("CUDA_VISIBLE_DEVICES") is None and os.path.exists("/dev/nvidia0"),
                     reason="a GPU is present")
 def test_no_device_fails_loudly():

@@ -54,6 +54,29 @@ def test_named_expval_batch(dtype):
 
 
 @pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("nq", [1, 3, 5, 8, 9, 10, 12, 14, 17, 22])
+def test_pauliz_sets_all_sizes(nq, dtype):
+    # PauliZ on every wire (each wire twice, in a shuffled order) and Identity:
+    # wires whose bits fall on lanes, steps and chunks of the one-pass
+    # reduction, and more values than one pass takes when nq >= 22
+    rng = np.random.default_rng(100 + nq)
+    psi = rand_state(nq, rng)
+    s = State.from_array(psi, dtype)
+    wires = list(rng.permutation(nq)) + list(range(nq)) + [0] * 3
+    names = ["PauliZ"] * (2 * nq) + ["Identity"] * 3
+    if nq >= 22:
+        wires += list(range(nq)) * 2
+        names += ["PauliZ"] * (2 * nq)
+    g = np.array([N.GATE_ID[n] for n in names], dtype=np.int32)
+    w, wp = i64(wires)
+    out = np.zeros(len(names))
+    N.check(N.lib.plk_expval_named_batch(s.h, len(names), g.ctypes.data_as(C.POINTER(C.c_int32)), wp,
+                                         out.ctypes.data_as(C.POINTER(C.c_double))))
+    for i, (n, ww) in enumerate(zip(names, wires)):
+        assert abs(out[i] - O.expval_named(psi, n, [int(ww)])) < ETOL[dtype], (n, ww)
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
 @pytest.mark.parametrize("k", [1, 2, 3, 4])
 def test_matrix_expval(k, dtype):
     rng = np.random.default_rng(10 + k)

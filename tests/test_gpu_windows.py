@@ -201,3 +201,50 @@ def test_window_adjoint_several_observables(dtype, nobs, window_switch):
     tol = 1e-10 if dtype == N.PLK_C128 else 1e-4
     np.testing.assert_allclose(jw, ref, atol=tol, rtol=0)
     np.testing.assert_allclose(jw, jp, atol=tol, rtol=0)
+
+
+def diagonal_heavy_circuit(nq, layers, rng, trainable_multi=True):
+    """Layers whose diagonal ops (RZ, PhaseShift, Z, S, T, CZ, CRZ, IsingZZ,
+    MultiRZ, ControlledPhaseShift) sit between rotations and CNOTs, including
+    repeated RZ on one wire: the complex128 windows merge such runs."""
+    ops = []
+    ang = lambda: [float(rng.uniform(0, 2 * np.pi))]  # noqa: E731
+    for _ in range(layers):
+        for w in range(nq):
+            ops.append(("RY", [w], False, ang()))
+            ops.append(("RZ", [w], bool(rng.integers(2)), ang()))
+            if w % 3 == 0:
+                ops.append(("RZ", [w], False, ang()))
+                ops.append(("PhaseShift", [w], bool(rng.integers(2)), ang()))
+            if w % 4 == 1:
+                ops.append((str(rng.choice(["PauliZ", "S", "T"])), [w], bool(rng.integers(2)), []))
+        for w in range(nq - 1):
+            ops.append(("CNOT", [w, w + 1], False, []))
+            if w % 3 == 1:
+                ops.append(("CZ", [w, w + 1], False, []))
+        a, b = (int(x) for x in rng.choice(nq, 2, replace=False))
+        ops.append(("CRZ", [a, b], False, ang()))
+        ops.append(("ControlledPhaseShift", [b, a], False, ang()))
+        if trainable_multi:
+            ops.append(("IsingZZ", [a, (a + 1) % nq], False, ang()))
+            ops.append(("MultiRZ", [int(x) for x in rng.choice(nq, 3, replace=False)], False, ang()))
+    return ops
+
+
+@pytest.mark.parametrize("nq", [7, 10, 13])
+def test_window_c128_diagonal_runs(nq, window_switch):
+    rng = np.random.default_rng(300 + nq)
+    ops = diagonal_heavy_circuit(nq, 3, rng)
+    window_switch(True)
+    a = run_forward(nq, ops, N.PLK_C128)
+    np.testing.assert_allclose(a, oracle_forward(nq, ops), atol=1e-12, rtol=0)
+    npar = sum(1 for o in ops if o[3])
+    trainable = sorted(int(x) for x in rng.choice(npar, npar * 3 // 4, replace=False))
+    obs = [("hamiltonian", [0.9, -0.6], [("named", "PauliX", [1]),
+                                         ("tensor", [("named", "PauliZ", [0]), ("named", "PauliY", [nq - 1])])])]
+    psi = O.run_ops(O.zero_state(nq), ops)
+    ref = O.adjoint_jacobian(psi, obs, ops, trainable)
+    jw = gpu_adjoint(psi, obs, ops, trainable, N.PLK_C128)
+    jw2 = gpu_adjoint(psi, obs, ops, trainable, N.PLK_C128)
+    np.testing.assert_array_equal(jw, jw2)
+    np.testing.assert_allclose(jw, ref, atol=1e-10, rtol=0)

@@ -41,12 +41,25 @@ def device_ptr(state):
     return p
 
 
+# value counts: the maximum (16) and counts that fill only part of the kernel
+# variant they run on (1, 3 -> 4, 5 -> 8, 9 -> 16), and the Identity alone
+WIRE_SETS = {
+    "16": list(range(15)) + [-1],
+    "1": [7],
+    "3": [0, 14, 6],
+    "5": [3, -1, 12, 1, 9],
+    "9": [8, 0, 2, 13, -1, 5, 11, 4, 14],
+    "identity": [-1],
+}
+
+
 @pytest.mark.parametrize("dtype", [N.PLK_C128, N.PLK_C64])
-def test_noalloc_matches_allocating_entry_point(dtype):
+@pytest.mark.parametrize("case", sorted(WIRE_SETS))
+def test_noalloc_matches_allocating_entry_point(dtype, case):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(42)
     nq = 15
-    wires = list(range(nq)) + [-1]  # 16 values: the maximum
+    wires = WIRE_SETS[case]
     out = torch.full((len(wires),), float("nan"), dtype=torch.float64, device="cuda")
     w, wp = i64(wires)
     for call in range(2):  # two calls in a row share the scratch array
@@ -57,8 +70,11 @@ def test_noalloc_matches_allocating_entry_point(dtype):
                                                 C.cast(C.c_void_p(out.data_ptr()), C.POINTER(C.c_double)),
                                                 C.c_void_p(torch.cuda.current_stream().cuda_stream)))
         torch.cuda.synchronize()
-        np.testing.assert_allclose(out.cpu().numpy(), ref, atol=ETOL[dtype], rtol=0, err_msg=f"call {call}")
-        assert abs(out[-1].item() - 1.0) < ETOL[dtype]
+        got = out.cpu().numpy()
+        np.testing.assert_allclose(got, ref, atol=ETOL[dtype], rtol=0, err_msg=f"call {call}")
+        for i, wi in enumerate(wires):
+            if wi < 0:  # Identity: the squared norm of a normalised state
+                assert abs(got[i] - 1.0) < ETOL[dtype]
 
 
 def test_noalloc_rejects_too_many_values():
