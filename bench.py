@@ -949,7 +949,7 @@ def run_kernels(args, device, torch):
         return sum(1 << (nq - 1 - x) for x, c in zip(w, l) if c in "XY")
 
     npass_words = len({xmask(w, l) for _, w, l in words})
-    m3, m2 = haar(3), haar(2)
+    m3, m2, m5, m6 = haar(3), haar(2), haar(5), haar(6)
     u = f64(rng.random(1 << 20))
     shots_out = np.empty((1 << 20) * nq, dtype=np.int64)
     probs_full = np.empty(n, dtype=np.float64)
@@ -1012,6 +1012,11 @@ def run_kernels(args, device, torch):
             ("MultiRZ (5 wires)", gate("MultiRZ", [0, 3, mid, lo, nq - 1], [0.8]), 2 * S),
             ("Haar 2-qubit matrix", matrix(m2, [mid, lo]), 2 * S),
             ("Haar 3-qubit matrix", matrix(m3, [hi, mid, lo]), 2 * S),
+            ("Haar 5-qubit matrix", matrix(m5, [hi, 4, mid, lo, nq - 1]), 2 * S),
+            ("Haar 6-qubit matrix", matrix(m6, [hi, 4, 7, mid, lo, nq - 1]), 2 * S),
+            ("Haar 6-qubit matrix, CUDA cores", lambda: (N.check(N.lib.plk_set_dense_tensor_cores(0)),
+                                                         matrix(m6, [hi, 4, 7, mid, lo, nq - 1])(),
+                                                         N.check(N.lib.plk_set_dense_tensor_cores(1))), 2 * S),
             ("generator IsingXX", lambda: N.check(N.lib.plk_apply_generator(a, N.GATE_ID["IsingXX"], P64(zw), 2, 0,
                                                                             C.byref(sc))), 2 * S),
             ("expval PauliZ", lambda: N.check(N.lib.plk_expval_named(a, N.GATE_ID["PauliZ"], P64(zw), 1,

@@ -267,6 +267,14 @@ enum { PLK_ARITH_DOUBLE_FLOAT = 0, PLK_ARITH_FP64 = 1 };
 PLK_API int plk_set_c128_arithmetic(int32_t mode);
 PLK_API int plk_get_c128_arithmetic(int32_t *mode);
 
+/* ---- tensor cores for dense complex64 matrices --------------------------- */
+/* complex64 dense matrices on 5 or 6 wires (plk_apply_matrix,
+ * applyMultiQubitOp, StateVectorKokkos.hpp:757-796) run on the tensor cores
+ * (TF32 operands, three products per step for FP32 accuracy) unless this is
+ * switched off; off, they run on the CUDA cores in FP32. */
+PLK_API int plk_set_dense_tensor_cores(int32_t enable);
+PLK_API int plk_get_dense_tensor_cores(int32_t *enabled);
+
 /* ---- gate matrices ---------------------------------------------------- */
 /* Dense matrix (row-major complex128 pairs, 4^num_wires of them; wires[0] is
  * the most significant bit of the row index) of a named gate, built from the

@@ -751,6 +751,10 @@ static int run_dense(plk_state s, const double *matrix, const int64_t *wires, in
     if (K == 3 || K == 4) return run_dense_reg<T>(s, hm, g, K);
     std::vector<uint64_t> hoff(dim);
     for (int i = 0; i < dim; i++) hoff[i] = g.local_off(i);
+    // complex64 on 5 or 6 wires: tensor cores (dense_tc.cu)
+    if constexpr (sizeof(T) == 4)
+        if ((K == 5 || K == 6) && dense_tc_enabled())
+            return launch_dense_tc(s, reinterpret_cast<const float2 *>(hm.data()), hoff.data(), g.mk, K);
     void *d_mat = nullptr, *d_off = nullptr;
     PLK_CUDA(cudaMallocAsync(&d_mat, hm.size() * sizeof(V), s->stream));
     PLK_CUDA(cudaMallocAsync(&d_off, hoff.size() * sizeof(uint64_t), s->stream));

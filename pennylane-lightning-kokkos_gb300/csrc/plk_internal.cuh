@@ -150,6 +150,12 @@ int fill_basis(plk_state s, uint64_t index);
 // (environment PLK_C128_ARITH=fp64).
 bool c128_use_df();
 
+// complex64 dense matrices on 5 or 6 wires on the tensor cores (dense_tc.cu)
+// unless plk_set_dense_tensor_cores(0)
+bool dense_tc_enabled();
+struct Masks;
+int launch_dense_tc(plk_state s, const float2 *U, const uint64_t *hoff, const Masks &gm, int K);
+
 // ----------------------------------------------------------------------------
 // complex arithmetic on float2 / double2
 // ----------------------------------------------------------------------------

@@ -103,6 +103,8 @@ _SIGS = {
     "plk_set_window_path": ([C.c_int32], C.c_int),
     "plk_get_window_path": ([_i32p], C.c_int),
     "plk_set_c128_arithmetic": ([C.c_int32], C.c_int),
+    "plk_set_dense_tensor_cores": ([C.c_int32], C.c_int),
+    "plk_get_dense_tensor_cores": ([_i32p], C.c_int),
     "plk_get_c128_arithmetic": ([_i32p], C.c_int),
     "plk_gate_matrix": ([C.c_int32, _dp, C.c_int32, C.c_int32, C.c_int32, _dp], C.c_int),
     "plk_batch_create": ([C.c_int32, C.c_int32, C.POINTER(_vp)], C.c_int),

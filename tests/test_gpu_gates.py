@@ -4,6 +4,7 @@ Tolerances: complex128 states within 1e-12 elementwise of the oracle;
 complex64 states within 5e-6 (single-precision rounding of a unit-norm state
 after one gate).
 """
+import ctypes as C
 import itertools
 
 import zlib
@@ -222,3 +223,35 @@ def test_invalid_arguments_are_rejected():
         s.apply("RX", [0], False, [])
     with pytest.raises(N.NativeError, match="at least one wire"):
         s.apply_matrix(np.eye(1), [])
+
+
+@pytest.fixture
+def dense_tc_switch():
+    old = C.c_int32()
+    N.check(N.lib.plk_get_dense_tensor_cores(C.byref(old)))
+    yield lambda on: N.check(N.lib.plk_set_dense_tensor_cores(int(on)))
+    N.check(N.lib.plk_set_dense_tensor_cores(old.value))
+
+
+@pytest.mark.parametrize("k", [5, 6])
+def test_dense_matrix_tensor_cores_c64(k, dense_tc_switch):
+    """complex64 matrices on 5 and 6 wires: the tensor-core kernel (TF32,
+    three products per step) against the CUDA-core kernel and the oracle on
+    15 qubits, wires at the highest, lowest and scattered bit positions,
+    unsorted; tolerance 5e-6 (single-precision rounding of the state)."""
+    rng = np.random.default_rng(600 + k)
+    nq = 15
+    for t, wires in enumerate((list(range(k)), list(range(nq - 1, nq - 1 - k, -1)),
+                               [int(w) for w in rng.choice(nq, k, False)])):
+        m = haar(1 << k, rng)
+        inverse = t == 2
+        psi = rand_state(nq, rng)
+        ref = O.apply_matrix(psi.copy(), m, wires, inverse)
+        out = {}
+        for on in (True, False):
+            dense_tc_switch(on)
+            s = State.from_array(psi, N.PLK_C64)
+            s.apply_matrix(m, wires, inverse)
+            out[on] = s.get()
+        np.testing.assert_allclose(out[True], ref, atol=5e-6, rtol=0, err_msg=f"tensor cores {wires}")
+        np.testing.assert_allclose(out[True], out[False], atol=5e-6, rtol=0, err_msg=f"tc vs cuda cores {wires}")
