@@ -23,7 +23,7 @@
 
 namespace plk {
 
-constexpr int kTcWarps = 4;
+constexpr int kTcWarps = 8;
 
 static std::atomic<int> g_dense_tc{1};
 bool dense_tc_enabled() { return g_dense_tc.load(std::memory_order_relaxed) != 0; }
@@ -163,7 +163,7 @@ int launch_dense_tc(plk_state s, const float2 *U, const uint64_t *hoff, const Ma
     if (e == cudaSuccess && device_ctx(s->device, &d) == PLK_OK) {
         const uint64_t tiles = (ngroups + 15) / 16;
         const size_t smem = K == 5 ? tc_smem_bytes<5>() : tc_smem_bytes<6>();
-        const int per_sm = K == 5 ? 3 : 1;
+        const int per_sm = K == 5 ? 3 : 1; // shared memory: 72 KB (K = 5), 207 KB (K = 6) per CTA
         const uint64_t want = (tiles + kTcWarps - 1) / kTcWarps;
         const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)d->sm_count * per_sm));
         const float *wh_d = (const float *)buf, *wl_d = (const float *)(buf + wbytes);
