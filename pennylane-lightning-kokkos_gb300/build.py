@@ -27,7 +27,7 @@ PKG = os.path.join(HERE, "pennylane_lightning_kokkos")
 OBJ = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
-CUDA_SOURCES = ["state.cu", "gates.cu", "expval.cu", "measure.cu", "adjoint.cu", "noalloc.cu", "batch.cu", "windows.cu", "windows_df.cu", "windows_df_fwd.cu", "adjoint_kinds2.cu", "adjoint_kinds3.cu", "dense_tc.cu"]
+CUDA_SOURCES = ["state.cu", "gates.cu", "expval.cu", "measure.cu", "adjoint.cu", "noalloc.cu", "batch.cu", "windows.cu", "windows_df.cu", "windows_df_fwd.cu", "adjoint_kinds2.cu", "adjoint_kinds3.cu", "dense_tc.cu", "windows_sms.cu"]
 BIND_SOURCES = ["bindings/Bindings.cpp"]
 LIB_NAME = "libplk_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -48,7 +48,7 @@ enum EKind : uint8_t {
     EK_DIAG = 3,  // diagonal gate on K <= 4 wires anywhere in the state
     EK_PARITY = 4, // MultiRZ: phase by parity of the state bits in a mask
     EK_DIAGSET = 5 // several diagonal ops on register bits merged into one 16-entry phase table
-                   // (complex128 single-state windows only): mat = the table; K = number of
+                   // (single-state windows only, not the batch engine): mat = the table; K = number of
                    // trainable one-wire members, member m in bits 8m.. of `bits` (register bit,
                    // generator codes of bit value 0 and 1: 0, 1 = +1, 2 = -1) and its reduction
                    // slot in bits 4m.. of `gen`

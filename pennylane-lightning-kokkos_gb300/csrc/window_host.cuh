@@ -220,7 +220,7 @@ struct WinBuilder {
     int64_t &n_mats;
     std::vector<double2> *hmats = nullptr; // when set: matrices from XOp::umat, written here (no EPrep)
     // merge runs of diagonal ops on register bits into EK_DIAGSET ops (needs
-    // hmats; only the complex128 single-state kernels implement the kind)
+    // hmats; only the single-state window kernels implement the kind)
     bool fuse_diag = false;
 
     std::vector<const XOp *> cur;

@@ -34,40 +34,12 @@ namespace plk {
 
 namespace {
 std::atomic<int> g_window_path{1};
-constexpr int kWinThreads = 256;
 } // namespace
 
-template <class T, bool BWD, bool SLIM>
-__global__ void __launch_bounds__(kWinThreads, 2)
-    k_state_window(c2_t<T> *lam, c2_t<T> *hl, int nq, const EWin *__restrict__ wins, int wi,
-                   const EOp *__restrict__ ops, const c2_t<T> *__restrict__ mats, const ETrain *__restrict__ train,
-                   double *__restrict__ bpart) {
-    using Slot = typename EAcc<T>::Slot;
-    __shared__ Slot part[kMaxWinTrain * kWinThreads];
-    const EWin w = wins[wi];
-    if (BWD)
-        for (int t = 0; t < w.ntrain; t++) part[t * kWinThreads + threadIdx.x] = Slot{};
-    run_window<T, kWinThreads, EM_GLOBAL, BWD, SLIM>(ops, mats, w, nq, lam, hl, blockIdx.x * kWinThreads + threadIdx.x,
-                                               gridDim.x * kWinThreads, part);
-    if (BWD && w.ntrain > 0) {
-        __syncthreads();
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        for (int t = warp; t < w.ntrain; t += kWinThreads / 32) {
-            EAcc<T> acc;
-#pragma unroll
-            for (int i = 0; i < kWinThreads / 32; i++) {
-                EAcc<T> x;
-                x.load(part[t * kWinThreads + i * 32 + lane]);
-                acc.merge(x);
-            }
-            const double s = acc.warp_sum();
-            if (lane == 0) {
-                const ETrain tr = train[w.tr0 + t];
-                bpart[(size_t)tr.slot * gridDim.x + blockIdx.x] = (double)tr.gscale * s;
-            }
-        }
-    }
-}
+// complex64 windows (windows_sms.cu: shared-memory staged, 128 threads per CTA)
+int window_sms_grid(int sm_count, uint64_t groups, bool bwd);
+void launch_window_sms(bool bwd, int grid, cudaStream_t st, float2 *lam, float2 *hl, int nq, const EWin *wins, int wi,
+                       int ntrain, const EOp *ops, const float2 *mats, const ETrain *train, double *bpart);
 
 // complex128 windows (windows_df.cu, windows_df_fwd.cu: shared-memory staged
 // double-float kernels, 128 threads per CTA)
@@ -215,10 +187,8 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
     PLK_TRY(device_ctx(lam->device, &d));
     cudaStream_t st = lam->stream;
     const uint64_t nu = lam->length >> kWinBits;
-    const int grid = std::is_same<T, double>::value
-                         ? window_df_grid(d->sm_count, nu, bwd)
-                         : (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)d->sm_count * 2,
-                                                                         (nu + kWinThreads - 1) / kWinThreads));
+    const int grid = std::is_same<T, double>::value ? window_df_grid(d->sm_count, nu, bwd)
+                                                     : window_sms_grid(d->sm_count, nu, bwd);
     // matrices: state precision for complex64, split double-floats for complex128
     using M = typename std::conditional<std::is_same<T, double>::value, float4, V>::type;
     std::vector<M> mats(P.mats.size() + P.gen.size());
@@ -273,8 +243,6 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
     V *lp = (V *)lam->data;
     V *hp = hl ? (V *)hl->data : nullptr;
     for (size_t wi = 0; wi < P.wins.size() && rc == PLK_OK; wi++) {
-        // windows of one-wire ops and CNOTs only run the slim kernel
-        const bool slim = P.wins[wi].flags & 1;
         if constexpr (std::is_same<T, double>::value) {
             const int in_df = wi > 0, out_df = wi + 1 < P.wins.size();
             if (bwd)
@@ -283,15 +251,9 @@ static int run_program(plk_state lam, plk_state hl, const StateProgram &P, bool 
             else
                 launch_window_df_fwd(grid, st, lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p, in_df, out_df);
         } else {
-#define PLK_W(B_, S_) k_state_window<T, B_, S_><<<grid, kWinThreads, 0, st>>>(lp, hp, lam->nq, d_w, (int)wi, d_o, d_m, d_t, d_p)
-            if (bwd) {
-                if (slim) PLK_W(true, true);
-                else PLK_W(true, false);
-            } else {
-                if (slim) PLK_W(false, true);
-                else PLK_W(false, false);
-            }
-#undef PLK_W
+            launch_window_sms(bwd, grid, st, reinterpret_cast<float2 *>(lp), reinterpret_cast<float2 *>(hp),
+                              lam->nq, d_w, (int)wi, P.wins[wi].ntrain, d_o, reinterpret_cast<const float2 *>(d_m), d_t,
+                              d_p);
         }
         if (cudaGetLastError() != cudaSuccess) rc = PLK_ERR_CUDA;
     }
@@ -332,7 +294,7 @@ int window_apply_ops(plk_state s, const plk_op *ops, int nops, bool &handled) {
     StateProgram P;
     WinBuilder wb{s->nq, false, P.wins, P.ops, P.train, P.prep, P.gen, P.n_mats};
     wb.hmats = &P.mats;
-    wb.fuse_diag = s->dtype == PLK_C128; // merged diagonal runs: complex128 kernels only
+    wb.fuse_diag = true; // merged diagonal runs (the single-state window kernels of both precisions)
     std::vector<const XOp *> seq;
     for (const auto &x : xs) seq.push_back(&x);
     PLK_TRY(wb.add_scheduled(seq));
@@ -382,7 +344,7 @@ int window_adjoint(plk_state lam, plk_state *hls, int nobs, const plk_op *ops, i
     StateProgram P;
     WinBuilder wb{lam->nq, true, P.wins, P.ops, P.train, P.prep, P.gen, P.n_mats};
     wb.hmats = &P.mats;
-    wb.fuse_diag = lam->dtype == PLK_C128; // merged diagonal runs: complex128 kernels only
+    wb.fuse_diag = true; // merged diagonal runs (the single-state window kernels of both precisions)
     std::vector<const XOp *> seq;
     for (const auto &x : xs) seq.push_back(&x);
     PLK_TRY(wb.add_scheduled(seq));
