@@ -376,6 +376,64 @@ __global__ void __launch_bounds__(kThreads) k_quad(c2_t<T> *__restrict__ sv, con
     }
 }
 
+// complex128 matrices on k >= 5 wires in double-float on the FP32 pipe: the
+// native-FP64 k_dense spends 4 FP64 instructions per complex multiply-add
+// (this GPU runs FP64 at about 1/64 of its FP32 rate).  The group vectors are
+// split into double-float pairs once, when they are staged in shared memory;
+// each thread forms one output row as a double-float complex dot product.
+// The matrix is stored transposed, [column][row] (split on the host), so the
+// threads of a warp (consecutive rows) read consecutive entries: no bank
+// conflicts; in shared memory for k <= 6, through L1/L2 beyond.
+constexpr int kSmemMatWiresDf = 6;
+
+__global__ void __launch_bounds__(kThreads) k_dense_df(double2 *__restrict__ sv, const float4 *__restrict__ matT,
+                                                       const uint64_t *__restrict__ off, Masks gm, int K,
+                                                       uint64_t ngroups, int mat_in_smem) {
+    extern __shared__ __align__(16) float4 dsm[];
+    const int dim = 1 << K;
+    float4 *smat = dsm;
+    float4 *svec = dsm + (mat_in_smem ? dim * dim : 0);
+    if (mat_in_smem)
+        for (int i = threadIdx.x; i < dim * dim; i += blockDim.x) smat[i] = matT[i];
+    const float4 *MT = mat_in_smem ? smat : matT;
+    const int gpb = dim >= kThreads ? 1 : kThreads / dim;
+    const int rows_per_thread = dim >= kThreads ? dim / kThreads : 1;
+    for (uint64_t gb = (uint64_t)blockIdx.x * gpb; gb < ngroups; gb += (uint64_t)gridDim.x * gpb) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < gpb * dim; t += blockDim.x) {
+            const int gi = t / dim, r = t % dim;
+            const uint64_t g = gb + gi;
+            if (g < ngroups) {
+                uint64_t base = g & gm.m[0];
+                for (int j = 1; j <= K; j++) base |= (g << j) & gm.m[j];
+                const CDF v = cdf_split(sv[base + off[r]]);
+                svec[t] = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo);
+            }
+        }
+        __syncthreads();
+        for (int rr = 0; rr < rows_per_thread; rr++) {
+            const int t = threadIdx.x + rr * kThreads;
+            const int gi = t / dim, r = t % dim;
+            const uint64_t g = gb + gi;
+            if (gi < gpb && g < ngroups) {
+                const float4 *vec = svec + gi * dim;
+                float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
+#pragma unroll 4
+                for (int j = 0; j < dim; j++) {
+                    const float4 m = MT[(size_t)j * dim + r], v = vec[j];
+                    df_mac(m.x, m.y, v.x, v.y, rh, rl);
+                    df_mac(-m.z, -m.w, v.z, v.w, rh, rl);
+                    df_mac(m.x, m.y, v.z, v.w, ih, il);
+                    df_mac(m.z, m.w, v.x, v.y, ih, il);
+                }
+                uint64_t base = g & gm.m[0];
+                for (int j = 1; j <= K; j++) base |= (g << j) & gm.m[j];
+                sv[base + off[r]] = make_double2(df_result(rh, rl), df_result(ih, il));
+            }
+        }
+    }
+}
+
 // MultiRZ: element-wise parity phase, four amplitudes in flight per thread
 constexpr int kMrzUnroll = 4;
 
@@ -755,6 +813,43 @@ static int run_dense(plk_state s, const double *matrix, const int64_t *wires, in
     if constexpr (sizeof(T) == 4)
         if ((K == 5 || K == 6) && dense_tc_enabled())
             return launch_dense_tc(s, reinterpret_cast<const float2 *>(hm.data()), hoff.data(), g.mk, K);
+    // complex128: double-float on the FP32 pipe unless native FP64 is requested
+    if constexpr (sizeof(T) == 8)
+        if (c128_use_df()) {
+            std::vector<float4> mt((size_t)dim * dim);
+            for (int r = 0; r < dim; r++)
+                for (int c = 0; c < dim; c++) {
+                    const V z = hm[(size_t)r * dim + c];
+                    float4 &f = mt[(size_t)c * dim + r];
+                    df_split_host(z.x, f.x, f.y);
+                    df_split_host(z.y, f.z, f.w);
+                }
+            const size_t mbytes = mt.size() * sizeof(float4), obytes = hoff.size() * sizeof(uint64_t);
+            char *buf = nullptr;
+            PLK_TRY(pool_alloc(s->device, (void **)&buf, mbytes + obytes, s->stream));
+            cudaError_t e = cudaMemcpyAsync(buf, mt.data(), mbytes, cudaMemcpyHostToDevice, s->stream);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(buf + mbytes, hoff.data(), obytes, cudaMemcpyHostToDevice, s->stream);
+            const uint64_t ngroups = s->length >> K;
+            const int mat_smem = K <= kSmemMatWiresDf ? 1 : 0;
+            const int gpb = dim >= kThreads ? 1 : kThreads / dim;
+            const size_t smem = (mat_smem ? mbytes : 0) + (size_t)gpb * dim * sizeof(float4);
+            DeviceCtx *d = nullptr;
+            if (e == cudaSuccess && smem > 48 * 1024)
+                e = cudaFuncSetAttribute(k_dense_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess && device_ctx(s->device, &d) == PLK_OK) {
+                const uint64_t want = (ngroups + gpb - 1) / gpb;
+                const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)d->sm_count * 8));
+                k_dense_df<<<grid, kThreads, smem, s->stream>>>((double2 *)s->data, (const float4 *)buf,
+                                                                 (const uint64_t *)(buf + mbytes), g.mk, K, ngroups,
+                                                                 mat_smem);
+                e = cudaGetLastError();
+            }
+            pool_free(buf, s->stream);
+            // the host staging vectors are released on return: make the copies finish
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+            if (e != cudaSuccess) PLK_FAIL(PLK_ERR_CUDA, std::string("dense matrix kernel: ") + cudaGetErrorString(e));
+            return PLK_OK;
+        }
     void *d_mat = nullptr, *d_off = nullptr;
     PLK_CUDA(cudaMallocAsync(&d_mat, hm.size() * sizeof(V), s->stream));
     PLK_CUDA(cudaMallocAsync(&d_off, hoff.size() * sizeof(uint64_t), s->stream));

@@ -161,3 +161,59 @@ class CircuitBatch:
         buf = C.create_string_buffer(8192)
         N.check(N.lib.plk_batch_tune(self._h, reps, buf, len(buf)))
         return buf.value.decode()
+
+
+# --------------------------------------------------------------- sharding --
+def shard_plan(costs: Sequence[float], world: int) -> list:
+    """Cost-balanced assignment of independent circuits to `world` GPUs:
+    circuits in decreasing cost (ties: lower index first), each to the GPU
+    with the least work so far (ties: lower rank).  `costs` are per-circuit
+    work estimates, e.g. gates x 2^qubits.  Returns, per rank, the circuit
+    indices it runs, in increasing order."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    order = sorted(range(len(costs)), key=lambda i: (-float(costs[i]), i))
+    load = [0.0] * world
+    shards = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        shards[r].append(i)
+        load[r] += float(costs[i])
+    return [sorted(s) for s in shards]
+
+
+def gather_shards(dist, shards: list, expvals, grads, root: int = 0):
+    """Reassembles per-rank results in circuit order on `root`: each rank
+    passes the expectation values and gradient arrays of its own shard (in
+    the shard's order).  The results travel once, as host objects, at the end
+    of a run (the circuits themselves need no exchange).  Returns
+    (expvals, grads) over all circuits on `root`, (None, None) elsewhere."""
+    rank = dist.get_rank()
+    payload = (list(map(float, expvals)), [np.asarray(g, dtype=np.float64) for g in grads])
+    gathered = [None] * dist.get_world_size() if rank == root else None
+    dist.gather_object(payload, gathered, dst=root)
+    if rank != root:
+        return None, None
+    n = sum(len(s) for s in shards)
+    ev_all, g_all = [None] * n, [None] * n
+    for r, (ev_r, g_r) in enumerate(gathered):
+        if len(ev_r) != len(shards[r]) or len(g_r) != len(shards[r]):
+            raise RuntimeError(f"rank {r} returned {len(ev_r)} results for a shard of {len(shards[r])} circuits")
+        for k, i in enumerate(shards[r]):
+            ev_all[i], g_all[i] = ev_r[k], g_r[k]
+    return np.array(ev_all), g_all
+
+
+def run_shard(workload: Sequence, shard: Sequence[int], dtype: str = "c64", device: int = 0):
+    """Runs this rank's circuits of `workload` ([(num_qubits, packed ops,
+    words)], as circuits.batch_workload_packed) in one CircuitBatch; returns
+    (expvals, gradients) in the shard's order."""
+    b = CircuitBatch(dtype, device)
+    try:
+        for i in shard:
+            nq, pk, words = workload[i]
+            b.add_packed(nq, pk, words)
+        ev, jac = b.run()
+        return ev, b.gradients(jac)
+    finally:
+        b.close()

@@ -290,3 +290,25 @@ def test_batch_errors():
     with pytest.raises(N.NativeError, match="Pauli letter"):
         b.add(5, [("RX", [0], False, [0.1])], [(1.0, [0], "Q")])
     b.close()
+
+
+def test_batch_shards_match_one_batch():
+    """A batch split by shard_plan into three shards, each run as its own
+    CircuitBatch (as three GPUs would), gives the results of one batch."""
+    from pennylane_lightning_kokkos.batch import CircuitBatch, run_shard, shard_plan
+    from pennylane_lightning_kokkos.circuits import batch_workload_packed
+
+    wl = batch_workload_packed(24, seed=11, min_qubits=4, max_qubits=9, min_layers=1, max_layers=4)
+    costs = [len(pk["gates"]) * float(1 << nq) for nq, pk, _ in wl]
+    b = CircuitBatch("c128")
+    for nq, pk, words in wl:
+        b.add_packed(nq, pk, words)
+    ev, jac = b.run()
+    grads = b.gradients(jac)
+    b.close()
+    shards = shard_plan(costs, 3)
+    for shard in shards:
+        ev_s, g_s = run_shard(wl, shard, "c128")
+        for k, i in enumerate(shard):
+            assert abs(ev_s[k] - ev[i]) < 1e-12
+            np.testing.assert_allclose(g_s[k], grads[i], atol=1e-12, rtol=0)

@@ -76,7 +76,7 @@ def test_gate_on_wide_state(name, mode):
         s.close()
 
 
-@pytest.mark.parametrize("k", [1, 2, 3, 4])
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
 def test_dense_matrix_on_wide_state(k, mode):
     rng = np.random.default_rng(40 + k)
     nq = 9

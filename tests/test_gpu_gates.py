@@ -255,3 +255,20 @@ def test_dense_matrix_tensor_cores_c64(k, dense_tc_switch):
             out[on] = s.get()
         np.testing.assert_allclose(out[True], ref, atol=5e-6, rtol=0, err_msg=f"tensor cores {wires}")
         np.testing.assert_allclose(out[True], out[False], atol=5e-6, rtol=0, err_msg=f"tc vs cuda cores {wires}")
+
+
+@pytest.mark.parametrize("dtype", DTYPES)
+@pytest.mark.parametrize("k", [5, 7])
+def test_dense_matrix_many_wires_large_state(k, dtype):
+    """5- and 7-wire matrices on 13 qubits (complex128: double-float kernel,
+    the 7-wire matrix read through L1/L2; complex64: tensor cores for 5 wires,
+    the CUDA-core kernel for 7)."""
+    rng = np.random.default_rng(700 + k)
+    nq = 13
+    for wires in (list(range(k)), [int(w) for w in rng.choice(nq, k, False)]):
+        m = haar(1 << k, rng)
+        psi = rand_state(nq, rng)
+        ref = O.apply_matrix(psi.copy(), m, wires, False)
+        s = State.from_array(psi, dtype)
+        s.apply_matrix(m, wires, False)
+        np.testing.assert_allclose(s.get(), ref, atol=TOL[dtype] * 4, rtol=0, err_msg=str(wires))
