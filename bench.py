@@ -16,7 +16,9 @@ Printed JSON line:
   value      - device-resident throughput (CUDA events on the state's stream)
   e2e        - the same metric through the reference-facing pybind API
                (LightningKokkos_C128) with the state copied from pinned host
-               memory before and back after every step
+               memory before and back after every step: two states on two
+               streams take alternate steps, so one step's copies overlap
+               the other's gates (`serial`: one state, blocking copies)
   roofline   - the gate kernel with the largest time share, against the
                measured HBM copy bandwidth
   per_gate   - GB/s and time share of every gate type (and wire range)
@@ -51,6 +53,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import gc
 import json
 import os
 import statistics
@@ -323,34 +326,92 @@ def fp64_pass(runner, groups, plan, amp, stream, torch, device):
 
 # -------------------------------------------------------------------- e2e --
 def run_e2e(args, device, torch, plan, steps):
+    """The sweep through the reference-facing module with host buffers: every
+    step copies a 2^n complex128 state in from pinned host memory, applies the
+    step's gates and copies the result back out.
+
+    Pipelined (the reported value): two states, each on its own CUDA stream,
+    take alternate steps; copies are queued (HostToDeviceAsync /
+    DeviceToHostAsync) and each step's gates start after the previous step's,
+    so one step's copies run while the other step's gates do.  Serial: one state, the blocking HostToDevice / DeviceToHost of the
+    reference API, one step at a time."""
     import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
 
     n = 1 << args.nq
-    host_t = torch.empty(n, dtype=torch.complex128, pin_memory=True)
-    host = host_t.numpy()
-    host[:] = 1.0 / np.sqrt(n)
-    sv = m.LightningKokkos_C128(args.nq, m.InitializationSettings().set_device_id(device))
-    names = [a["name"] for a in plan]
     amp = 2 * n * 16
+    step_bytes = sum(a["touched"] * amp for a in plan)
+    names = [a["name"] for a in plan]
+    inp = torch.empty(n, dtype=torch.complex128, pin_memory=True).numpy()
+    inp[:] = 1.0 / np.sqrt(n)
+    outs = [torch.empty(n, dtype=torch.complex128, pin_memory=True).numpy() for _ in range(2)]
 
-    def one_step():
-        sv.HostToDevice(host)
+    def gates(sv):
         for a in plan:
             if a["matrix"] is not None:
                 sv.apply("QubitUnitary", a["wires"], False, [[]], a["matrix"])
             else:
                 getattr(sv, a["name"])(a["wires"], False, a["params"])
-        sv.DeviceToHost(host)
 
-    one_step()  # warm-up
+    settings = m.InitializationSettings().set_device_id(device)
+    # serial: the reference API's blocking copies
+    sv = m.LightningKokkos_C128(args.nq, settings)
+
+    def serial_step():
+        sv.HostToDevice(inp)
+        gates(sv)
+        sv.DeviceToHost(outs[0])
+
+    serial_step()  # warm-up
     t = time.perf_counter()
     for _ in range(steps):
-        one_step()
-    dt = time.perf_counter() - t
-    nbytes = sum(a["touched"] * amp for a in plan) * steps
+        serial_step()
+    serial_s = (time.perf_counter() - t) / steps
     del sv
-    return {"value": nbytes / dt / 1e9, "unit": "GB/s", "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": n * 16,
-            "steps": steps, "api": "lightning_kokkos_qubit_ops.LightningKokkos_C128 (pinned host buffer)",
+    # pipelined: two states on two streams
+    streams = [torch.cuda.Stream(device=device) for _ in range(2)]
+    svs = [m.LightningKokkos_C128(args.nq, settings) for _ in range(2)]
+    for k in range(2):
+        svs[k].set_stream(streams[k].cuda_stream)
+
+    # a step's gates wait for the previous step's gates (an event between the
+    # streams): the two states never compete for the SMs, so one state's
+    # copies run while the other's gates do instead of both copying at once
+    done = [torch.cuda.Event(), torch.cuda.Event()]
+
+    def queue_step(k):
+        s = svs[k % 2]
+        s.HostToDeviceAsync(inp)
+        if k > 0:
+            streams[k % 2].wait_event(done[(k - 1) % 2])
+        gates(s)
+        done[k % 2].record(streams[k % 2])
+        s.DeviceToHostAsync(outs[k % 2])
+
+    for k in range(2):  # warm-up
+        queue_step(k)
+    for s in svs:
+        s.synchronize()
+    psteps = max(10, 2 * steps)  # the first copy in and the last copy out are not overlapped: amortise them
+    t = time.perf_counter()
+    for k in range(psteps):
+        queue_step(k)
+    for s in svs:
+        s.synchronize()
+    pipe_s = (time.perf_counter() - t) / psteps
+    del svs
+    del inp, outs  # release the pinned buffers (torch caches them otherwise)
+    gc.collect()
+    if hasattr(torch._C, "_host_emptyCache"):
+        torch._C._host_emptyCache()
+    return {"value": step_bytes / pipe_s / 1e9, "unit": "GB/s", "h2d_bytes_per_step": n * 16,
+            "d2h_bytes_per_step": n * 16, "steps": psteps, "s_per_step": pipe_s,
+            "api": "lightning_kokkos_qubit_ops.LightningKokkos_C128: HostToDeviceAsync, gates, DeviceToHostAsync "
+                   "(pinned host buffers)",
+            "pipeline": "two states on two CUDA streams take alternate steps; each step's gates wait for the previous "
+                        "step's, and its copies overlap the other step's gates; host wall clock from the first "
+                        "queued copy to the last result in host memory",
+            "serial": {"value": step_bytes / serial_s / 1e9, "s_per_step": serial_s, "steps": steps,
+                       "api": "LightningKokkos_C128.HostToDevice, gates, DeviceToHost (blocking, one state)"},
             "gates_per_step": len(names)}
 
 

@@ -134,6 +134,13 @@ PLK_API int plk_state_set_values(plk_state s, const uint64_t *indices, const voi
  * precision). */
 PLK_API int plk_state_h2d(plk_state s, const void *host, uint64_t length);
 PLK_API int plk_state_d2h(plk_state s, void *host, uint64_t length);
+/* The same copies without the wait: queued on the state's stream after the
+ * work already queued there, and returning at once.  The host buffer must
+ * stay valid (and, for d2h, unread) until plk_state_synchronize; with pinned
+ * host memory and a stream per state, one state's copies overlap another
+ * state's gates. */
+PLK_API int plk_state_h2d_async(plk_state s, const void *host, uint64_t length);
+PLK_API int plk_state_d2h_async(plk_state s, void *host, uint64_t length);
 /* DeviceToDevice / updateData :1596-1598, :1631-1633 */
 PLK_API int plk_state_copy(plk_state dst, plk_state src);
 /* axpy_Kokkos (util/LinearAlgebraKokkos.hpp:30-61): y += alpha * x */

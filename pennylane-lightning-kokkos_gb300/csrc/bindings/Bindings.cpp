@@ -189,9 +189,30 @@ template <class PrecisionT, class ParamT> void bind_precision(py::module_ &m) {
         .def("numQubits", &SV::getNumQubits)
         .def("dataLength", &SV::getLength)
         .def("resetKokkos", &SV::resetStateVector)
-        // GB300 additions: raw device pointer (for zero-copy interop) and the
-        // Pauli-sum expectation value
+        // GB300 additions: raw device pointer (for zero-copy interop), queued
+        // host copies and the stream they go on, and the Pauli-sum
+        // expectation value
         .def("device_ptr", [](SV &sv) { return (uintptr_t)sv.devicePtr(); })
+        .def(
+            "HostToDeviceAsync",
+            [](SV &sv, py::array_t<std::complex<PrecisionT>, py::array::c_style> &host) {
+                if (host.size()) sv.HostToDeviceAsync(host.data(), (size_t)host.size());
+            },
+            py::arg("host").noconvert(),
+            "Queue the host-to-device copy on the state's stream and return; the array (of the state's dtype: no "
+            "conversion copy is made) must stay alive and unchanged until synchronize().")
+        .def(
+            "DeviceToHostAsync",
+            [](SV &sv, py::array_t<std::complex<PrecisionT>, py::array::c_style> &host) {
+                if (host.size()) sv.DeviceToHostAsync(host.mutable_data(), (size_t)host.size());
+            },
+            py::arg("host").noconvert(),
+            "Queue the device-to-host copy on the state's stream and return; read the array after synchronize().")
+        .def(
+            "set_stream", [](SV &sv, uintptr_t stream) { sv.setStream((void *)stream); },
+            "Queue this state's work on a CUDA stream (an address such as torch.cuda.Stream().cuda_stream; 0: the "
+            "library's stream).")
+        .def("synchronize", [](SV &sv) { sv.synchronize(); }, "Wait for this state's queued work.")
         .def("ExpectationValuePauliSum",
              [](SV &sv, const std::vector<double> &coeffs, const std::vector<std::vector<size_t>> &wires,
                 const std::vector<std::string> &letters) {

@@ -110,6 +110,12 @@ template <class PrecisionT> class StateVectorGB {
     void resetStateVector() { check(plk_state_reset(h_)); }
     void HostToDevice(const ComplexT *sv, size_t length) { check(plk_state_h2d(h_, sv, length)); }
     void DeviceToHost(ComplexT *sv, size_t length) const { check(plk_state_d2h(h_, sv, length)); }
+    // Queued copies (no wait; the buffer stays in use until synchronize())
+    void HostToDeviceAsync(const ComplexT *sv, size_t length) { check(plk_state_h2d_async(h_, sv, length)); }
+    void DeviceToHostAsync(ComplexT *sv, size_t length) const { check(plk_state_d2h_async(h_, sv, length)); }
+    // The CUDA stream this state's work is queued on (nullptr: the library's)
+    void setStream(void *stream) { check(plk_state_set_stream(h_, stream)); }
+    void synchronize() const { check(plk_state_synchronize(h_)); }
     void DeviceToDevice(const StateVectorGB &other) { check(plk_state_copy(h_, other.h_)); }
     void updateData(const StateVectorGB &other) { DeviceToDevice(other); }
 

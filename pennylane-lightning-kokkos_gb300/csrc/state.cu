@@ -493,6 +493,24 @@ PLK_API int plk_state_d2h(plk_state s, void *host, uint64_t length) {
     return PLK_OK;
 }
 
+PLK_API int plk_state_h2d_async(plk_state s, const void *host, uint64_t length) {
+    PLK_TRY(check_state(s));
+    if (length != s->length) PLK_FAIL(PLK_ERR_INVALID_ARG, "length does not match the state size");
+    if (!host) PLK_FAIL(PLK_ERR_INVALID_ARG, "null host buffer");
+    PLK_CUDA(cudaSetDevice(s->device));
+    PLK_CUDA(cudaMemcpyAsync(s->data, host, length * amp_bytes(s->dtype), cudaMemcpyHostToDevice, s->stream));
+    return PLK_OK;
+}
+
+PLK_API int plk_state_d2h_async(plk_state s, void *host, uint64_t length) {
+    PLK_TRY(check_state(s));
+    if (length != s->length) PLK_FAIL(PLK_ERR_INVALID_ARG, "length does not match the state size");
+    if (!host) PLK_FAIL(PLK_ERR_INVALID_ARG, "null host buffer");
+    PLK_CUDA(cudaSetDevice(s->device));
+    PLK_CUDA(cudaMemcpyAsync(host, s->data, length * amp_bytes(s->dtype), cudaMemcpyDeviceToHost, s->stream));
+    return PLK_OK;
+}
+
 PLK_API int plk_state_copy(plk_state dst, plk_state src) {
     PLK_TRY(check_state(dst));
     PLK_TRY(check_state(src));

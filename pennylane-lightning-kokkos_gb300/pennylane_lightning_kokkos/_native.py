@@ -76,6 +76,8 @@ _SIGS = {
     "plk_state_set_values": ([_vp, C.POINTER(C.c_uint64), _vp, C.c_uint64], C.c_int),
     "plk_state_h2d": ([_vp, _vp, C.c_uint64], C.c_int),
     "plk_state_d2h": ([_vp, _vp, C.c_uint64], C.c_int),
+    "plk_state_h2d_async": ([_vp, _vp, C.c_uint64], C.c_int),
+    "plk_state_d2h_async": ([_vp, _vp, C.c_uint64], C.c_int),
     "plk_state_copy": ([_vp, _vp], C.c_int),
     "plk_state_axpy": ([_vp, C.c_double, C.c_double, _vp], C.c_int),
     "plk_apply_gate": ([_vp, C.c_int32, _i64p, C.c_int32, C.c_int32, _dp, C.c_int32], C.c_int),

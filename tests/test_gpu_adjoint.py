@@ -173,3 +173,41 @@ def test_pybind_known_answers():
         np.testing.assert_allclose(got, expected, rtol=tol, atol=tol, err_msg=case)
     with pytest.raises(m.PLException):
         sv3.RX([5], False, [0.1])
+
+
+@pytest.mark.parametrize("bits", ["64", "128"])
+def test_pybind_queued_copies_two_streams(bits):
+    """HostToDeviceAsync / DeviceToHostAsync on two states with their own
+    streams, interleaved with gates: each state ends as the oracle's."""
+    import torch
+
+    import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
+
+    cls = getattr(m, "LightningKokkos_C" + bits)
+    cdt = np.complex128 if bits == "128" else np.complex64
+    tol = 1e-12 if bits == "128" else 1e-5
+    nq = 12
+    rng = np.random.default_rng(41)
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    svs = [cls(nq), cls(nq)]
+    ins, outs, refs = [], [], []
+    for k in range(2):
+        svs[k].set_stream(streams[k].cuda_stream)
+        psi = rand_state(nq, rng)
+        ins.append(torch.from_numpy(psi.astype(cdt)).pin_memory().numpy())
+        outs.append(torch.zeros(1 << nq, dtype=torch.complex128 if bits == "128" else torch.complex64).pin_memory()
+                    .numpy())
+        ops = [("RX", [k + 1], False, [0.3 + k]), ("CNOT", [k, 7], False, []), ("IsingXX", [2, 9], False, [0.7])]
+        refs.append((psi, ops))
+    for k in range(2):
+        svs[k].HostToDeviceAsync(ins[k])
+    for k in range(2):
+        for name, w, inv, p in refs[k][1]:
+            getattr(svs[k], name)(w, inv, p)
+        svs[k].DeviceToHostAsync(outs[k])
+    for k in range(2):
+        svs[k].synchronize()
+        ref = O.run_ops(refs[k][0].astype(cdt).astype(np.complex128), refs[k][1])
+        np.testing.assert_allclose(outs[k], ref, atol=tol)
+    with pytest.raises(TypeError):  # no silent conversion copy for a queued copy
+        svs[0].HostToDeviceAsync(np.zeros(1 << nq, dtype=np.complex64 if bits == "128" else np.complex128))
