@@ -16,9 +16,9 @@ Printed JSON line:
   value      - device-resident throughput (CUDA events on the state's stream)
   e2e        - the same metric through the reference-facing pybind API
                (LightningKokkos_C128) with the state copied from pinned host
-               memory before and back after every step: two states on two
-               streams take alternate steps, so one step's copies overlap
-               the other's gates (`serial`: one state, blocking copies)
+               memory before and back after every step: three states on
+               three streams take steps in turn, so a step's copies overlap
+               other steps' gates (`serial`: one state, blocking copies)
   roofline   - the gate kernel with the largest time share, against the
                measured HBM copy bandwidth
   per_gate   - GB/s and time share of every gate type (and wire range)
@@ -330,10 +330,11 @@ def run_e2e(args, device, torch, plan, steps):
     step copies a 2^n complex128 state in from pinned host memory, applies the
     step's gates and copies the result back out.
 
-    Pipelined (the reported value): two states, each on its own CUDA stream,
-    take alternate steps; copies are queued (HostToDeviceAsync /
+    Pipelined (the reported value): three states, each on its own CUDA
+    stream, take steps in turn; copies are queued (HostToDeviceAsync /
     DeviceToHostAsync) and each step's gates start after the previous step's,
-    so one step's copies run while the other step's gates do.  Serial: one state, the blocking HostToDevice / DeviceToHost of the
+    so a state's copies out and in run while the other two states' gates do
+    (two gate periods of slack for a host link whose rate varies).  Serial: one state, the blocking HostToDevice / DeviceToHost of the
     reference API, one step at a time."""
     import pennylane_lightning_kokkos.lightning_kokkos_qubit_ops as m
 
@@ -343,7 +344,8 @@ def run_e2e(args, device, torch, plan, steps):
     names = [a["name"] for a in plan]
     inp = torch.empty(n, dtype=torch.complex128, pin_memory=True).numpy()
     inp[:] = 1.0 / np.sqrt(n)
-    outs = [torch.empty(n, dtype=torch.complex128, pin_memory=True).numpy() for _ in range(2)]
+    P = 3  # states in the pipeline
+    outs = [torch.empty(n, dtype=torch.complex128, pin_memory=True).numpy() for _ in range(P)]
 
     def gates(sv):
         for a in plan:
@@ -367,27 +369,28 @@ def run_e2e(args, device, torch, plan, steps):
         serial_step()
     serial_s = (time.perf_counter() - t) / steps
     del sv
-    # pipelined: two states on two streams
-    streams = [torch.cuda.Stream(device=device) for _ in range(2)]
-    svs = [m.LightningKokkos_C128(args.nq, settings) for _ in range(2)]
-    for k in range(2):
+    # pipelined: P states on P streams
+    streams = [torch.cuda.Stream(device=device) for _ in range(P)]
+    svs = [m.LightningKokkos_C128(args.nq, settings) for _ in range(P)]
+    for k in range(P):
         svs[k].set_stream(streams[k].cuda_stream)
 
     # a step's gates wait for the previous step's gates (an event between the
-    # streams): the two states never compete for the SMs, so one state's
-    # copies run while the other's gates do instead of both copying at once
-    done = [torch.cuda.Event(), torch.cuda.Event()]
+    # streams): the states never compete for the SMs, so a state's copies run
+    # while the others' gates do instead of all copying at once
+    done = [torch.cuda.Event() for _ in range(P)]
 
     def queue_step(k):
-        s = svs[k % 2]
+        i = k % P
+        s = svs[i]
         s.HostToDeviceAsync(inp)
         if k > 0:
-            streams[k % 2].wait_event(done[(k - 1) % 2])
+            streams[i].wait_event(done[(k - 1) % P])
         gates(s)
-        done[k % 2].record(streams[k % 2])
-        s.DeviceToHostAsync(outs[k % 2])
+        done[i].record(streams[i])
+        s.DeviceToHostAsync(outs[i])
 
-    for k in range(2):  # warm-up
+    for k in range(P):  # warm-up
         queue_step(k)
     for s in svs:
         s.synchronize()
@@ -407,8 +410,8 @@ def run_e2e(args, device, torch, plan, steps):
             "d2h_bytes_per_step": n * 16, "steps": psteps, "s_per_step": pipe_s,
             "api": "lightning_kokkos_qubit_ops.LightningKokkos_C128: HostToDeviceAsync, gates, DeviceToHostAsync "
                    "(pinned host buffers)",
-            "pipeline": "two states on two CUDA streams take alternate steps; each step's gates wait for the previous "
-                        "step's, and its copies overlap the other step's gates; host wall clock from the first "
+            "pipeline": f"{P} states on {P} CUDA streams take steps in turn; each step's gates wait for the previous "
+                        "step's, and a state's copies overlap the other states' gates; host wall clock from the first "
                         "queued copy to the last result in host memory",
             "serial": {"value": step_bytes / serial_s / 1e9, "s_per_step": serial_s, "steps": steps,
                        "api": "LightningKokkos_C128.HostToDevice, gates, DeviceToHost (blocking, one state)"},
