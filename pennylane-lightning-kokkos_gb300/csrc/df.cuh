@@ -106,6 +106,71 @@ inline void df_split_host(double x, float &hi, float &lo) {
     lo = (float)(x - (double)hi);
 }
 
+// ---- two lanes per instruction --------------------------------------------
+// PTX .f32x2 arithmetic (sm_100 and later) runs two independent FP32
+// operations in one instruction; each lane is rounded exactly as the scalar
+// instruction.  A complex double-float accumulator is carried as two packed
+// pairs, (re.hi, im.hi) and (re.lo, im.lo), so the real and imaginary
+// chains of a complex multiply-add share instructions.  Lane 0 is the low
+// 32 bits (the first float of mov.b64 {a, b}).
+typedef unsigned long long f2x;
+
+__device__ __forceinline__ f2x f2x_pack(float a, float b) {
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2x_unpack(f2x v, float &a, float &b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2x f2x_add(f2x a, f2x b) {
+    f2x r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x f2x_sub(f2x a, f2x b) {
+    f2x r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x f2x_mul(f2x a, f2x b) {
+    f2x r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2x f2x_fma(f2x a, f2x b, f2x c) {
+    f2x r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// Packed df_mac: (sh, sl) += a * b in both lanes, a given as ah and the
+// negated pair (nah, nal) = -(ah, al).  The error chain is carried negated,
+// en = -e (round-to-nearest is symmetric, so en is exactly the negative of
+// df_mac's e at every step), which needs no negation instructions; each
+// lane's result is bit for bit df_mac's.
+__device__ __forceinline__ void df_mac2(f2x ah, f2x nah, f2x nal, f2x bh, f2x bl, f2x &sh, f2x &sl) {
+    const f2x p = f2x_mul(ah, bh);
+    f2x en = f2x_fma(nah, bh, p);
+    en = f2x_fma(nah, bl, en);
+    en = f2x_fma(nal, bh, en);
+    const f2x s = f2x_add(sh, p);
+    const f2x bb = f2x_sub(s, sh);
+    const f2x t = f2x_add(f2x_sub(sh, f2x_sub(s, bb)), f2x_sub(p, bb));
+    sh = s;
+    sl = f2x_add(sl, f2x_sub(t, en));
+}
+
+// Packed df_first: (sh, sl) = a * b (the low part as 0 - en: a zero low
+// part may differ from df_first's in sign only)
+__device__ __forceinline__ void df_first2(f2x ah, f2x nah, f2x nal, f2x bh, f2x bl, f2x &sh, f2x &sl) {
+    sh = f2x_mul(ah, bh);
+    f2x en = f2x_fma(nah, bh, sh);
+    en = f2x_fma(nah, bl, en);
+    en = f2x_fma(nal, bh, en);
+    sl = f2x_sub(0ull, en);
+}
+
 // Complex double-float amplitude
 struct CDF {
     DF re, im;

@@ -13,6 +13,8 @@
 // (simulator/GateFunctors.hpp); FMA contraction is allowed.
 #pragma once
 
+#include <cstring>
+
 #include "df.cuh"
 #include "plk_internal.cuh"
 
@@ -305,6 +307,62 @@ template <class T> struct QuadArgs {
     uint64_t off[4];
     T coef[32];
     float ch[32], cl[32];
+    // complex128 4x4 matrix on the packed (re, im) double-float path: per
+    // entry m = mr + i mi, the pairs (mr, mr) and (-mi, mi) (hi), and their
+    // negations (hi and lo) -- see quad_mat_df2
+    f2x pk[6][16];
 };
+
+// Fills QuadArgs::pk from the double-float split coefficients (ch, cl).
+inline void quad_pack_host(const float *ch, const float *cl, f2x (&pk)[6][16]) {
+    auto bits = [](float f) {
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        return (f2x)u;
+    };
+    auto pack = [&](float lane0, float lane1) { return bits(lane0) | (bits(lane1) << 32); };
+    for (int e = 0; e < 16; e++) {
+        const float rh = ch[2 * e], rl = cl[2 * e], ih = ch[2 * e + 1], il = cl[2 * e + 1];
+        pk[0][e] = pack(rh, rh);   // A term: (mr, mr) * (v.re, v.im)
+        pk[1][e] = pack(-rh, -rh);
+        pk[2][e] = pack(-rl, -rl);
+        pk[3][e] = pack(-ih, ih);  // B term: (-mi, mi) * (v.im, v.re)
+        pk[4][e] = pack(ih, -ih);
+        pk[5][e] = pack(il, -il);
+    }
+}
+
+// The 4x4 complex128 matrix in double-float with the real and imaginary
+// chains packed two lanes per instruction: lane by lane the same operations,
+// in the same order, as df_cdot<4> (each output's real part accumulates
+// mr*v.re then -mi*v.im per column, its imaginary part mr*v.im then mi*v.re).
+__device__ __forceinline__ void quad_mat_df2(double2 (&v)[4], const f2x (&pk)[6][16]) {
+    f2x vh[4], vl[4], wh[4], wl[4]; // v = (re, im), w = (im, re)
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const CDF a = cdf_split(v[i]);
+        vh[i] = f2x_pack(a.re.hi, a.im.hi);
+        vl[i] = f2x_pack(a.re.lo, a.im.lo);
+        wh[i] = f2x_pack(a.im.hi, a.re.hi);
+        wl[i] = f2x_pack(a.im.lo, a.re.lo);
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        f2x sh, sl;
+        const int e0 = 4 * r;
+        df_first2(pk[0][e0], pk[1][e0], pk[2][e0], vh[0], vl[0], sh, sl);
+        df_mac2(pk[3][e0], pk[4][e0], pk[5][e0], wh[0], wl[0], sh, sl);
+#pragma unroll
+        for (int c = 1; c < 4; c++) {
+            const int e = e0 + c;
+            df_mac2(pk[0][e], pk[1][e], pk[2][e], vh[c], vl[c], sh, sl);
+            df_mac2(pk[3][e], pk[4][e], pk[5][e], wh[c], wl[c], sh, sl);
+        }
+        float rh, ih, rl, il;
+        f2x_unpack(sh, rh, ih);
+        f2x_unpack(sl, rl, il);
+        v[r] = make_double2(df_result(rh, rl), df_result(ih, il));
+    }
+}
 
 } // namespace plk

@@ -369,7 +369,8 @@ __global__ void __launch_bounds__(kThreads) k_quad(c2_t<T> *__restrict__ sv, con
         V v[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) v[i] = sv[base + a.off[i]];
-        if constexpr (DFP) quad_op_df<OP>(v, a.ch, a.cl);
+        if constexpr (DFP && OP == Q_MAT) quad_mat_df2(v, a.pk);
+        else if constexpr (DFP) quad_op_df<OP>(v, a.ch, a.cl);
         else quad_op<OP>(v, a.coef);
 #pragma unroll
         for (int i = 0; i < 4; i++) sv[base + a.off[i]] = v[i];
@@ -697,6 +698,7 @@ template <class T> static int run_quad(plk_state s, const GatePlan &p, const Wir
         a.coef[j] = (T)p.coef[j];
         df_split_host(p.coef[j], a.ch[j], a.cl[j]);
     }
+    quad_pack_host(a.ch, a.cl, a.pk);
     const int grid = gate_grid<T>(s, a.ngroups, 1);
     switch (p.op) {
     case Q_IXX: launch_quad_op<T, Q_IXX>(s, grid, a); break;
