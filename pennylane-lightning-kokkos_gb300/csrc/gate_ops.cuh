@@ -314,21 +314,28 @@ template <class T> struct QuadArgs {
 };
 
 // Fills QuadArgs::pk from the double-float split coefficients (ch, cl).
-inline void quad_pack_host(const float *ch, const float *cl, f2x (&pk)[6][16]) {
+// The six packed words of one matrix entry m = (rh + rl) + i (ih + il):
+// A = (mr, mr), its negation (hi, lo), B = (-mi, mi), its negation (hi, lo).
+inline void pack_entry_host(float rh, float rl, float ih, float il, f2x (&w)[6]) {
     auto bits = [](float f) {
         uint32_t u;
         std::memcpy(&u, &f, 4);
         return (f2x)u;
     };
     auto pack = [&](float lane0, float lane1) { return bits(lane0) | (bits(lane1) << 32); };
+    w[0] = pack(rh, rh); // A term: (mr, mr) * (v.re, v.im)
+    w[1] = pack(-rh, -rh);
+    w[2] = pack(-rl, -rl);
+    w[3] = pack(-ih, ih); // B term: (-mi, mi) * (v.im, v.re)
+    w[4] = pack(ih, -ih);
+    w[5] = pack(il, -il);
+}
+
+inline void quad_pack_host(const float *ch, const float *cl, f2x (&pk)[6][16]) {
     for (int e = 0; e < 16; e++) {
-        const float rh = ch[2 * e], rl = cl[2 * e], ih = ch[2 * e + 1], il = cl[2 * e + 1];
-        pk[0][e] = pack(rh, rh);   // A term: (mr, mr) * (v.re, v.im)
-        pk[1][e] = pack(-rh, -rh);
-        pk[2][e] = pack(-rl, -rl);
-        pk[3][e] = pack(-ih, ih);  // B term: (-mi, mi) * (v.im, v.re)
-        pk[4][e] = pack(ih, -ih);
-        pk[5][e] = pack(il, -il);
+        f2x w[6];
+        pack_entry_host(ch[2 * e], cl[2 * e], ch[2 * e + 1], cl[2 * e + 1], w);
+        for (int q = 0; q < 6; q++) pk[q][e] = w[q];
     }
 }
 

@@ -504,10 +504,16 @@ __global__ void __launch_bounds__(kThreads)
                 const float2 *__restrict__ mat_f) {
     constexpr int D = 1 << K;
     using V = c2_t<T>;
-    __shared__ __align__(16) float4 m4[sizeof(T) == 8 ? D * D : 1];
+    // complex128: packed double-float (two lanes per instruction), per entry
+    // three 16-byte words {A.h, A.nh}, {A.nl, B.h}, {B.nh, B.nl} with
+    // A = (mr, mr), B = (-mi, mi) (pack_entry_host)
+    constexpr bool PK = sizeof(T) == 8;
+    __shared__ __align__(16) float4 m4[sizeof(T) == 8 && !PK ? D * D : 1];
+    __shared__ __align__(16) ulonglong2 mp[PK ? 3 * D * D : 1];
     __shared__ __align__(8) float2 m2[sizeof(T) == 8 ? 1 : D * D];
-    for (int i = threadIdx.x; i < D * D; i += blockDim.x) {
-        if constexpr (sizeof(T) == 8) m4[i] = mat_df[i];
+    for (int i = threadIdx.x; i < (PK ? 3 : 1) * D * D; i += blockDim.x) {
+        if constexpr (PK) mp[i] = reinterpret_cast<const ulonglong2 *>(mat_df)[i];
+        else if constexpr (sizeof(T) == 8) m4[i] = mat_df[i];
         else m2[i] = mat_f[i];
     }
     __syncthreads();
@@ -519,7 +525,33 @@ __global__ void __launch_bounds__(kThreads)
         V v[D];
 #pragma unroll
         for (int i = 0; i < D; i++) v[i] = sv[base + a.off[i]];
-        if constexpr (sizeof(T) == 8) {
+        if constexpr (PK) {
+            f2x vh[D], vl[D], wh[D], wl[D]; // v = (re, im), w = (im, re)
+#pragma unroll
+            for (int i = 0; i < D; i++) {
+                const CDF c = cdf_split(v[i]);
+                vh[i] = f2x_pack(c.re.hi, c.im.hi);
+                vl[i] = f2x_pack(c.re.lo, c.im.lo);
+                wh[i] = f2x_pack(c.im.hi, c.re.hi);
+                wl[i] = f2x_pack(c.im.lo, c.re.lo);
+            }
+#pragma unroll
+            for (int r = 0; r < D; r++) {
+                f2x sh, sl;
+#pragma unroll
+                for (int c = 0; c < D; c++) {
+                    const ulonglong2 q0 = mp[3 * (r * D + c)], q1 = mp[3 * (r * D + c) + 1],
+                                     q2 = mp[3 * (r * D + c) + 2];
+                    if (c == 0) df_first2(q0.x, q0.y, q1.x, vh[0], vl[0], sh, sl);
+                    else df_mac2(q0.x, q0.y, q1.x, vh[c], vl[c], sh, sl);
+                    df_mac2(q1.y, q2.x, q2.y, wh[c], wl[c], sh, sl);
+                }
+                float rh, ih, rl, il;
+                f2x_unpack(sh, rh, ih);
+                f2x_unpack(sl, rl, il);
+                sv[base + a.off[r]] = make_double2(df_result(rh, rl), df_result(ih, il));
+            }
+        } else if constexpr (sizeof(T) == 8) {
             CDF w[D];
 #pragma unroll
             for (int i = 0; i < D; i++) w[i] = cdf_split(v[i]);
@@ -760,8 +792,10 @@ static int launch_dense_reg(plk_state s, const std::vector<c2_t<T>> &hm, const W
     a.mk = g.mk;
     a.ngroups = s->length >> K;
     for (int i = 0; i < D; i++) a.off[i] = g.local_off(i);
+    constexpr bool PK = sizeof(T) == 8; // packed double-float (k_dense_reg)
     std::vector<float4> mdf(sizeof(T) == 8 ? D * D : 0);
     std::vector<float2> mf(sizeof(T) == 8 ? 0 : D * D);
+    std::vector<f2x> mpk(PK ? 6 * D * D : 0);
     for (int i = 0; i < D * D; i++) {
         if constexpr (sizeof(T) == 8) {
             df_split_host(hm[i].x, mdf[i].x, mdf[i].y);
@@ -770,11 +804,19 @@ static int launch_dense_reg(plk_state s, const std::vector<c2_t<T>> &hm, const W
             mf[i] = make_float2((float)hm[i].x, (float)hm[i].y);
         }
     }
-    const size_t bytes = sizeof(T) == 8 ? sizeof(float4) * D * D : sizeof(float2) * D * D;
+    if constexpr (PK) {
+        // per entry {A.h, A.nh}, {A.nl, B.h}, {B.nh, B.nl}; A = (mr, mr), B = (-mi, mi)
+        for (int i = 0; i < D * D; i++) {
+            f2x w[6];
+            pack_entry_host(mdf[i].x, mdf[i].y, mdf[i].z, mdf[i].w, w);
+            std::copy(w, w + 6, mpk.begin() + 6 * i);
+        }
+    }
+    const size_t bytes = PK ? sizeof(f2x) * mpk.size() : sizeof(T) == 8 ? sizeof(float4) * D * D : sizeof(float2) * D * D;
     void *d_mat = nullptr;
     PLK_TRY(pool_alloc(s->device, &d_mat, bytes, s->stream));
-    cudaError_t e = cudaMemcpyAsync(d_mat, sizeof(T) == 8 ? (const void *)mdf.data() : (const void *)mf.data(), bytes,
-                                    cudaMemcpyHostToDevice, s->stream);
+    const void *src = PK ? (const void *)mpk.data() : sizeof(T) == 8 ? (const void *)mdf.data() : (const void *)mf.data();
+    cudaError_t e = cudaMemcpyAsync(d_mat, src, bytes, cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) {
         const unsigned grid = (unsigned)((a.ngroups + kThreads - 1) / kThreads);
         k_dense_reg<T, K><<<grid, kThreads, 0, s->stream>>>((c2_t<T> *)s->data, a, (const float4 *)d_mat,
