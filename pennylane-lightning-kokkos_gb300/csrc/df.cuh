@@ -123,6 +123,12 @@ __device__ __forceinline__ f2x f2x_pack(float a, float b) {
 __device__ __forceinline__ void f2x_unpack(f2x v, float &a, float &b) {
     asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
 }
+// (b, a) from (a, b)
+__device__ __forceinline__ f2x f2x_swap(f2x v) {
+    float a, b;
+    f2x_unpack(v, a, b);
+    return f2x_pack(b, a);
+}
 __device__ __forceinline__ f2x f2x_add(f2x a, f2x b) {
     f2x r;
     asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
@@ -168,6 +174,28 @@ __device__ __forceinline__ void df_first2(f2x ah, f2x nah, f2x nal, f2x bh, f2x 
     f2x en = f2x_fma(nah, bh, sh);
     en = f2x_fma(nah, bl, en);
     en = f2x_fma(nal, bh, en);
+    sl = f2x_sub(0ull, en);
+}
+
+// df_mac2 / df_first2 with the negation on the other factor: b given as bh
+// and (nbh, nbl) = -(bh, bl), for a data-dependent a reused against
+// several b (the same operations lane by lane: fma(a, -b, p) = fma(-a, b, p)).
+__device__ __forceinline__ void df_mac2n(f2x ah, f2x al, f2x bh, f2x nbh, f2x nbl, f2x &sh, f2x &sl) {
+    const f2x p = f2x_mul(ah, bh);
+    f2x en = f2x_fma(ah, nbh, p);
+    en = f2x_fma(ah, nbl, en);
+    en = f2x_fma(al, nbh, en);
+    const f2x s = f2x_add(sh, p);
+    const f2x bb = f2x_sub(s, sh);
+    const f2x t = f2x_add(f2x_sub(sh, f2x_sub(s, bb)), f2x_sub(p, bb));
+    sh = s;
+    sl = f2x_add(sl, f2x_sub(t, en));
+}
+__device__ __forceinline__ void df_first2n(f2x ah, f2x al, f2x bh, f2x nbh, f2x nbl, f2x &sh, f2x &sl) {
+    sh = f2x_mul(ah, bh);
+    f2x en = f2x_fma(ah, nbh, sh);
+    en = f2x_fma(ah, nbl, en);
+    en = f2x_fma(al, nbh, en);
     sl = f2x_sub(0ull, en);
 }
 

@@ -89,22 +89,46 @@ template <int K> struct HermArgs {
     uint64_t off[D];
     float dh[D], dl[D];         // H_rr
     float ah[P], al[P], bh[P], bl[P];
+    // complex128 packed form (herm_group_df2): per diagonal entry (d, d) and
+    // per pair (a, b), each as {hi, -hi, -lo}
+    f2x pd[D][3], pab[P][3];
 };
 
-// the r < c pair terms of a complex128 group, unrolled at compile time
-template <int D, int R, int C, int K>
-__device__ __forceinline__ void herm_pairs_df(const CDF (&w)[D], const HermArgs<K> &a, DAcc &acc) {
-    if constexpr (R < D - 1) {
-        constexpr int P = R * D - R * (R + 1) / 2 + (C - R - 1); // index of (R, C) among r < c pairs
-        float xh, xl, yh, yl;
-        df_first(w[R].re.hi, w[R].re.lo, w[C].re.hi, w[C].re.lo, xh, xl);
-        df_mac(w[R].im.hi, w[R].im.lo, w[C].im.hi, w[C].im.lo, xh, xl);
-        df_first(w[R].re.hi, w[R].re.lo, w[C].im.hi, w[C].im.lo, yh, yl);
-        df_mac(-w[R].im.hi, -w[R].im.lo, w[C].re.hi, w[C].re.lo, yh, yl);
-        df_mac(a.ah[P], a.al[P], xh, xl, acc.h, acc.l);
-        df_mac(a.bh[P], a.bl[P], yh, yl, acc.h, acc.l);
-        if constexpr (C + 1 < D) herm_pairs_df<D, R, C + 1>(w, a, acc);
-        else herm_pairs_df<D, R + 1, R + 2>(w, a, acc);
+// <v|H|v> of one complex128 group, real and imaginary lanes packed (df.cuh):
+// the pair term (x, y) = (Re, Im-like) of conj(w_r) w_c is one packed
+// double-float, weighted by (a, b); |w_r|^2 as the lanes (re^2, im^2)
+// weighted by (d, d).  pa collects both lanes.
+template <int K>
+__device__ __forceinline__ void herm_group_df2(const double2 (&v)[1 << K], const HermArgs<K> &a, f2x &ph, f2x &pl) {
+    constexpr int D = 1 << K;
+    f2x vh[D], vl[D], nvh[D], nvl[D];
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+        const CDF c = cdf_split(v[i]);
+        vh[i] = f2x_pack(c.re.hi, c.im.hi);
+        vl[i] = f2x_pack(c.re.lo, c.im.lo);
+        nvh[i] = f2x_pack(-c.re.hi, -c.im.hi);
+        nvl[i] = f2x_pack(-c.re.lo, -c.im.lo);
+    }
+#pragma unroll
+    for (int r = 0; r < D; r++) {
+        f2x nh, nl; // (re^2, im^2)
+        df_first2n(vh[r], vl[r], vh[r], nvh[r], nvl[r], nh, nl);
+        df_mac2(a.pd[r][0], a.pd[r][1], a.pd[r][2], nh, nl, ph, pl);
+        float rh, ih, rl, il;
+        f2x_unpack(vh[r], rh, ih);
+        f2x_unpack(vl[r], rl, il);
+        const f2x arh = f2x_pack(rh, rh), arl = f2x_pack(rl, rl); // (w_r.re, w_r.re)
+        const f2x brh = f2x_pack(ih, -ih), brl = f2x_pack(il, -il); // (w_r.im, -w_r.im)
+#pragma unroll
+        for (int c = r + 1; c < D; c++) {
+            const int P = r * D - r * (r + 1) / 2 + (c - r - 1); // index of (r, c) among r < c pairs
+            // x = w_r.re w_c.re + w_r.im w_c.im, y = w_r.re w_c.im - w_r.im w_c.re
+            f2x xh, xl;
+            df_first2n(arh, arl, vh[c], nvh[c], nvl[c], xh, xl);
+            df_mac2n(brh, brl, f2x_swap(vh[c]), f2x_swap(nvh[c]), f2x_swap(nvl[c]), xh, xl);
+            df_mac2(a.pab[P][0], a.pab[P][1], a.pab[P][2], xh, xl, ph, pl);
+        }
     }
 }
 
@@ -115,6 +139,7 @@ __global__ void __launch_bounds__(kThreads)
     constexpr int D = 1 << K;
     constexpr int UG = K == 1 ? 4 : (K == 2 ? 2 : 1); // groups in flight per thread
     DAcc acc;
+    f2x ph = 0ull, pl = 0ull; // complex128: packed lanes (herm_group_df2)
     const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t g0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g0 < a.ngroups; g0 += step * UG) {
         c2_t<T> v[UG][D];
@@ -142,17 +167,16 @@ __global__ void __launch_bounds__(kThreads)
                     }
                 acc.add(DF{t, 0.0f});
             } else {
-                CDF w[D];
-#pragma unroll
-                for (int i = 0; i < D; i++) w[i] = to_cdf(v[u][i]);
-#pragma unroll
-                for (int r = 0; r < D; r++) {
-                    const DF n = df_norm2(w[r]);
-                    df_mac(a.dh[r], a.dl[r], n.hi, n.lo, acc.h, acc.l);
-                }
-                herm_pairs_df<D, 0, 1>(w, a, acc);
+                herm_group_df2<K>(v[u], a, ph, pl);
             }
         }
+    }
+    if constexpr (sizeof(T) == 8) {
+        float h0, h1, l0, l1;
+        f2x_unpack(ph, h0, h1);
+        f2x_unpack(pl, l0, l1);
+        df_add(h0, l0, acc.h, acc.l);
+        df_add(h1, l1, acc.h, acc.l);
     }
     double r[1] = {acc.value()};
     block_reduce_finish<1>(r, partials, result, counter);
@@ -725,6 +749,23 @@ static int expval_herm_impl(plk_state s, const double *matrix, const int64_t *wi
             df_split_host(2.0 * hre, a.ah[p], a.al[p]);
             df_split_host(-2.0 * him, a.bh[p], a.bl[p]);
         }
+    // packed pairs {(x0, x1), -(x0, x1) hi, -(x0, x1) lo} for herm_group_df2
+    auto bits = [](float f) {
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        return (f2x)u;
+    };
+    auto pack = [&](float l0, float l1) { return bits(l0) | (bits(l1) << 32); };
+    for (int r = 0; r < D; r++) {
+        a.pd[r][0] = pack(a.dh[r], a.dh[r]);
+        a.pd[r][1] = pack(-a.dh[r], -a.dh[r]);
+        a.pd[r][2] = pack(-a.dl[r], -a.dl[r]);
+    }
+    for (int q = 0; q < p; q++) {
+        a.pab[q][0] = pack(a.ah[q], a.bh[q]);
+        a.pab[q][1] = pack(-a.ah[q], -a.bh[q]);
+        a.pab[q][2] = pack(-a.al[q], -a.bl[q]);
+    }
     const int grid = red_grid_k(s, k_expval_herm<T, K>, a.ngroups);
     auto &w = s->ws;
     k_expval_herm<T, K><<<grid, kThreads, 0, s->stream>>>((const c2_t<T> *)s->data, a, w.d_partials, w.d_result,
