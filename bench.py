@@ -72,8 +72,8 @@ METRIC = "gate HBM GB/s vs peak; adjoint grad s/circuit c64+FP64-acc vs c128 at 
 # what bounds a gate kernel below the HBM roofline (from its ncu profile)
 KERNEL_LIMITS = {
     "Haar2q": "FP32-pipe issue: the complex128 4x4 matrix runs in double-float, 16 error-free multiply-adds "
-              "per amplitude (about 275 FP32 instructions); DRAM traffic equals the algorithmic bytes; the "
-              "complex64 kernel runs at the copy rate",
+              "per amplitude with the real and imaginary lanes packed two per instruction (.f32x2); DRAM "
+              "traffic equals the algorithmic bytes; the complex64 kernel runs at the copy rate",
 }
 GIB = 1 << 30
 
