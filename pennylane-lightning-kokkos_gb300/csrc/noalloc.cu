@@ -43,41 +43,33 @@ std::mutex g_noalloc_mutex;
 void *g_noalloc_ptr[64] = {nullptr};
 } // namespace
 
-// The same one-pass kernel as the regular entry points (expval_diag.cuh),
-// with its partial sums and ticket counter in the fixed scratch array and
-// the result written to the caller's buffer.  The grid is the kernel's
-// resident blocks per SM times the SM count (at most kNoAllocMaxBlocks),
-// found with the occupancy API, which allocates nothing.
-template <class T, int NV>
-static int launch_noalloc(const void *state, uint64_t n, const DiagMasks &zm, int nv, unsigned char *scr, double *out,
+// The same one-pass kernel as the regular entry points for single-wire
+// PauliZ / Identity values (k_expval_zbits, expval_diag.cuh), with its
+// partial sums (value v of block b at v * grid + b) and ticket counter in the
+// fixed scratch array and the results written to the caller's buffer.  The
+// grid is the kernel's resident blocks per SM times the SM count (at most
+// kNoAllocMaxBlocks), found with the occupancy API, which allocates nothing.
+template <class T>
+static int launch_noalloc(const void *state, uint64_t n, const ZBits &zb, int nv, unsigned char *scr, double *out,
                           cudaStream_t st, int sms) {
+    constexpr int M = sizeof(T) == 4 ? 5 : 4; // steps per lane per chunk: 2^M
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_expval_diag<T, NV>, kThreads, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_expval_zbits<T, M>, kThreads, 0) != cudaSuccess ||
         occ < 1) {
         cudaGetLastError();
         occ = 1;
     }
-    const uint64_t nquads = ((n + 127) >> 7) << 5;
-    uint64_t grid = (nquads + kThreads - 1) / kThreads;
+    const uint64_t chunks = (n + ((uint64_t)32 << M) - 1) / ((uint64_t)32 << M);
+    uint64_t grid = (chunks * 32 + kThreads - 1) / kThreads; // one warp per chunk
     const uint64_t cap = std::min<uint64_t>((uint64_t)kNoAllocMaxBlocks, (uint64_t)sms * (uint64_t)occ);
     if (grid > cap) grid = cap;
     if (grid < 1) grid = 1;
     auto *counter = reinterpret_cast<unsigned int *>(scr);
     auto *partials = reinterpret_cast<double *>(scr + kNoAllocCounterBytes);
-    k_expval_diag<T, NV><<<(unsigned)grid, kThreads, 0, st>>>((const c2_t<T> *)state, n, zm, nv, partials, out,
+    k_expval_zbits<T, M><<<(unsigned)grid, kThreads, 0, st>>>((const c2_t<T> *)state, n, zb, nv, partials, out,
                                                               counter);
     PLK_CHECK_LAUNCH();
     return PLK_OK;
-}
-
-template <class T>
-static int noalloc_dispatch(const void *state, uint64_t n, const DiagMasks &zm, int nv, unsigned char *scr,
-                            double *out, cudaStream_t st, int sms) {
-    if (nv == 1) return launch_noalloc<T, 1>(state, n, zm, nv, scr, out, st, sms);
-    if (nv == 2) return launch_noalloc<T, 2>(state, n, zm, nv, scr, out, st, sms);
-    if (nv <= 4) return launch_noalloc<T, 4>(state, n, zm, nv, scr, out, st, sms);
-    if (nv <= 8) return launch_noalloc<T, 8>(state, n, zm, nv, scr, out, st, sms);
-    return launch_noalloc<T, 16>(state, n, zm, nv, scr, out, st, sms);
 }
 
 static int noalloc_scratch(int device, void **out) {
@@ -114,11 +106,11 @@ PLK_API int plk_expval_pauliz_noalloc(const void *state, int32_t num_qubits, int
                                           std::to_string(kNoAllocMaxValues) + " values per call");
     if (((uintptr_t)state) % amp_bytes(dtype) != 0 || ((uintptr_t)out) % sizeof(double) != 0)
         PLK_FAIL(PLK_ERR_INVALID_ARG, "misaligned state or output pointer");
-    DiagMasks zm{};
+    ZBits zb{};
     for (int i = 0; i < count; i++) {
         if (wires[i] < -1 || wires[i] >= num_qubits)
             PLK_FAIL(PLK_ERR_INVALID_ARG, "wire " + std::to_string(wires[i]) + " out of range (-1 = Identity)");
-        zm.z[i] = wires[i] < 0 ? 0ULL : (1ULL << (num_qubits - 1 - wires[i]));
+        zb.b[i] = wires[i] < 0 ? (int8_t)-1 : (int8_t)(num_qubits - 1 - wires[i]);
     }
     int device = 0;
     PLK_CUDA(cudaGetDevice(&device));
@@ -131,8 +123,8 @@ PLK_API int plk_expval_pauliz_noalloc(const void *state, int32_t num_qubits, int
     cudaStream_t st = (cudaStream_t)cuda_stream;
     PLK_CUDA(cudaMemsetAsync(scratch, 0, kNoAllocCounterBytes, st)); // ticket counter starts at zero
     auto *scr = static_cast<unsigned char *>(scratch);
-    return dtype == PLK_C64 ? noalloc_dispatch<float>(state, n, zm, count, scr, out, st, sms)
-                            : noalloc_dispatch<double>(state, n, zm, count, scr, out, st, sms);
+    return dtype == PLK_C64 ? launch_noalloc<float>(state, n, zb, count, scr, out, st, sms)
+                            : launch_noalloc<double>(state, n, zb, count, scr, out, st, sms);
 }
 
 } // extern "C"
