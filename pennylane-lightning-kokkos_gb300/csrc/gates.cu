@@ -14,9 +14,13 @@
 //   k_mrz   — element-wise parity phase (MultiRZ and its generator;
 //             k_mrz_df for complex128 in double-float);
 //   k_dense_reg — 2^k x 2^k matrices for k = 3, 4: one group per thread in
-//             registers, matrix in shared memory;
-//   k_dense — k >= 5, group vectors staged in shared memory, matrix in
-//             shared memory when it fits.
+//             registers, matrix in shared memory (complex128 in packed
+//             double-float);
+//   k_dense_df — complex128, k >= 5, in double-float;
+//   k_dense — complex64 k >= 7 (5 and 6 run on the tensor cores,
+//             dense_tc.cu) and complex128 k >= 3 in native-FP64 mode; group
+//             vectors staged in shared memory, matrix in shared memory when
+//             it fits.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -500,20 +504,18 @@ template <int K> struct DenseRegArgs {
 
 template <class T, int K>
 __global__ void __launch_bounds__(kThreads)
-    k_dense_reg(c2_t<T> *__restrict__ sv, const DenseRegArgs<K> a, const float4 *__restrict__ mat_df,
+    k_dense_reg(c2_t<T> *__restrict__ sv, const DenseRegArgs<K> a, const ulonglong2 *__restrict__ mat_pk,
                 const float2 *__restrict__ mat_f) {
     constexpr int D = 1 << K;
     using V = c2_t<T>;
     // complex128: packed double-float (two lanes per instruction), per entry
     // three 16-byte words {A.h, A.nh}, {A.nl, B.h}, {B.nh, B.nl} with
-    // A = (mr, mr), B = (-mi, mi) (pack_entry_host)
+    // A = (mr, mr), B = (-mi, mi) (pack_entry_host), passed as mat_pk
     constexpr bool PK = sizeof(T) == 8;
-    __shared__ __align__(16) float4 m4[sizeof(T) == 8 && !PK ? D * D : 1];
     __shared__ __align__(16) ulonglong2 mp[PK ? 3 * D * D : 1];
-    __shared__ __align__(8) float2 m2[sizeof(T) == 8 ? 1 : D * D];
+    __shared__ __align__(8) float2 m2[PK ? 1 : D * D];
     for (int i = threadIdx.x; i < (PK ? 3 : 1) * D * D; i += blockDim.x) {
-        if constexpr (PK) mp[i] = reinterpret_cast<const ulonglong2 *>(mat_df)[i];
-        else if constexpr (sizeof(T) == 8) m4[i] = mat_df[i];
+        if constexpr (PK) mp[i] = mat_pk[i];
         else m2[i] = mat_f[i];
     }
     __syncthreads();
@@ -549,23 +551,6 @@ __global__ void __launch_bounds__(kThreads)
                 float rh, ih, rl, il;
                 f2x_unpack(sh, rh, ih);
                 f2x_unpack(sl, rl, il);
-                sv[base + a.off[r]] = make_double2(df_result(rh, rl), df_result(ih, il));
-            }
-        } else if constexpr (sizeof(T) == 8) {
-            CDF w[D];
-#pragma unroll
-            for (int i = 0; i < D; i++) w[i] = cdf_split(v[i]);
-#pragma unroll
-            for (int r = 0; r < D; r++) {
-                float rh = 0.0f, rl = 0.0f, ih = 0.0f, il = 0.0f;
-#pragma unroll
-                for (int c = 0; c < D; c++) {
-                    const float4 e = m4[r * D + c];
-                    df_mac(e.x, e.y, w[c].re.hi, w[c].re.lo, rh, rl);
-                    df_mac(-e.z, -e.w, w[c].im.hi, w[c].im.lo, rh, rl);
-                    df_mac(e.x, e.y, w[c].im.hi, w[c].im.lo, ih, il);
-                    df_mac(e.z, e.w, w[c].re.hi, w[c].re.lo, ih, il);
-                }
                 sv[base + a.off[r]] = make_double2(df_result(rh, rl), df_result(ih, il));
             }
         } else {
@@ -819,7 +804,7 @@ static int launch_dense_reg(plk_state s, const std::vector<c2_t<T>> &hm, const W
     cudaError_t e = cudaMemcpyAsync(d_mat, src, bytes, cudaMemcpyHostToDevice, s->stream);
     if (e == cudaSuccess) {
         const unsigned grid = (unsigned)((a.ngroups + kThreads - 1) / kThreads);
-        k_dense_reg<T, K><<<grid, kThreads, 0, s->stream>>>((c2_t<T> *)s->data, a, (const float4 *)d_mat,
+        k_dense_reg<T, K><<<grid, kThreads, 0, s->stream>>>((c2_t<T> *)s->data, a, (const ulonglong2 *)d_mat,
                                                             (const float2 *)d_mat);
         e = cudaGetLastError();
     }
@@ -850,7 +835,9 @@ static int run_dense(plk_state s, const double *matrix, const int64_t *wires, in
         }
     WireGeom g;
     wire_geom(s->nq, wires, K, g);
-    if (K == 3 || K == 4) return run_dense_reg<T>(s, hm, g, K);
+    // 3 and 4 wires: one group per thread (complex128 in packed double-float;
+    // native-FP64 mode takes the generic kernel below)
+    if ((K == 3 || K == 4) && (sizeof(T) == 4 || c128_use_df())) return run_dense_reg<T>(s, hm, g, K);
     std::vector<uint64_t> hoff(dim);
     for (int i = 0; i < dim; i++) hoff[i] = g.local_off(i);
     // complex64 on 5 or 6 wires: tensor cores (dense_tc.cu)
