@@ -153,8 +153,9 @@ __device__ __forceinline__ f2x f2x_fma(f2x a, f2x b, f2x c) {
 // Packed df_mac: (sh, sl) += a * b in both lanes, a given as ah and the
 // negated pair (nah, nal) = -(ah, al).  The error chain is carried negated,
 // en = -e (round-to-nearest is symmetric, so en is exactly the negative of
-// df_mac's e at every step), which needs no negation instructions; each
-// lane's result is bit for bit df_mac's.
+// df_mac's e at every step, up to the sign of a zero), which needs no
+// negation instructions; each lane's result is df_mac's bit for bit (a zero
+// may differ in sign).
 __device__ __forceinline__ void df_mac2(f2x ah, f2x nah, f2x nal, f2x bh, f2x bl, f2x &sh, f2x &sl) {
     const f2x p = f2x_mul(ah, bh);
     f2x en = f2x_fma(nah, bh, p);
