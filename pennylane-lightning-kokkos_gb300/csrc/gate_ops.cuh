@@ -244,10 +244,8 @@ __device__ __forceinline__ void quad_op_df(double2 (&v)[4], const float *__restr
         CDF a[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) a[i] = cdf_split(v[i]);
-        if constexpr (OP == Q_MAT) {
-#pragma unroll
-            for (int r = 0; r < 4; r++) v[r] = df_cdot<4>(h + 8 * r, l + 8 * r, a);
-        } else if constexpr (OP == Q_IXX) {
+        static_assert(OP != Q_MAT, "the 4x4 matrix runs packed (quad_mat_df2)");
+        if constexpr (OP == Q_IXX) {
             // (cr v.re + sj w.im, cr v.im - sj w.re) with w the flipped partner
 #pragma unroll
             for (int i = 0; i < 4; i++) {
@@ -341,8 +339,9 @@ inline void quad_pack_host(const float *ch, const float *cl, f2x (&pk)[6][16]) {
 
 // The 4x4 complex128 matrix in double-float with the real and imaginary
 // chains packed two lanes per instruction: lane by lane the same operations,
-// in the same order, as df_cdot<4> (each output's real part accumulates
-// mr*v.re then -mi*v.im per column, its imaginary part mr*v.im then mi*v.re).
+// in the same order, as df_cdot<4> would issue (each output's real part
+// accumulates mr*v.re then -mi*v.im per column, its imaginary part mr*v.im
+// then mi*v.re).
 __device__ __forceinline__ void quad_mat_df2(double2 (&v)[4], const f2x (&pk)[6][16]) {
     f2x vh[4], vl[4], wh[4], wl[4]; // v = (re, im), w = (im, re)
 #pragma unroll
